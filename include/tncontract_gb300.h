@@ -1,0 +1,182 @@
+/*
+ * tncontract_gb300 -- C ABI of the GB300 (sm_103a) engine for tncontract's
+ * tensor-network hot path.
+ *
+ * The reference library (andrewdarmawan/tncontract) is pure Python on NumPy:
+ * it has no FFI layer of its own.  Every entry point below replaces one NumPy
+ * / LAPACK call (or one loop body) that the reference's Python code makes on
+ * the hot path; each declaration cites that call site (path within the
+ * reference project, file:line).  A binding layer (ctypes in this project,
+ * see tncontract_gb300/_lib.py) calls these with device pointers it owns.
+ *
+ * Conventions
+ *  - All pointers are device pointers unless stated otherwise; matrices are
+ *    row-major (C order, like NumPy's default) with explicit leading
+ *    dimensions; tensors are dense C-order arrays.
+ *  - `dtype` is one of TNC_F32 / TNC_F64 / TNC_C64 / TNC_C128; complex values
+ *    are (re, im) pairs like numpy.complex64 / complex128.
+ *  - Scalars (alpha, beta) are passed as host `double[2]` = (re, im).
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).
+ *  - Functions return a TNC_* status; they never allocate device memory.
+ *    Factorisations take a caller-provided workspace whose size is given by
+ *    the matching *_workspace_size function.
+ *  - Device-side failures (non-convergence, non-finite input, barrier
+ *    timeout) are written to a device `info` word that the caller reads
+ *    after synchronising; nothing traps or spins without bound.
+ */
+#ifndef TNCONTRACT_GB300_H
+#define TNCONTRACT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { TNC_F32 = 0, TNC_F64 = 1, TNC_C64 = 2, TNC_C128 = 3 };
+
+enum {
+  TNC_OK = 0,
+  TNC_ERR_ARG = 1,           /* bad shape / dtype / pointer argument       */
+  TNC_ERR_NOT_CONVERGED = 2, /* Jacobi sweep cap reached                   */
+  TNC_ERR_NONFINITE = 3,     /* NaN / Inf met in the input                 */
+  TNC_ERR_CUDA = 4,          /* a CUDA launch or API call failed           */
+  TNC_ERR_WORKSPACE = 5,     /* workspace smaller than *_workspace_size    */
+  TNC_ERR_TIMEOUT = 6        /* a bounded device-side wait gave up         */
+};
+
+/* matrix operation applied to a row-major operand */
+enum { TNC_OP_N = 0, TNC_OP_T = 1, TNC_OP_C = 2 /* conj-transpose */, TNC_OP_R = 3 /* conj */ };
+
+int tnc_abi_version(void);
+const char *tnc_status_string(int status);
+
+/* ------------------------------------------------------------ data movement */
+
+/* dst = transpose(src, perm) (optionally conjugated): dst.shape[i] =
+ * shape[perm[i]].  rank <= 8.  Replaces the axis moves of the reference:
+ * np.rollaxis in Tensor.move_index / move_indices / consolidate_indices
+ * (tncontract/tensor.py:340-394, 396-482) and the operand transposes inside
+ * np.tensordot (tensor.py:735); conj=1 replaces Tensor.conjugate
+ * (tensor.py:484-485). */
+int tnc_permute(int dtype, const void *src, void *dst, int rank,
+                const int64_t *shape, const int *perm, int conj, void *stream);
+
+/* y[i] = alpha * (conj ? conj(x[i]) : x[i]); x may equal y.  Replaces
+ * Tensor.__mul__/__rmul__ (tensor.py:95-123) and the in-place rescalings of
+ * the MPS routines (onedim_core.py:301-314, 357-358, 479-484). */
+int tnc_scale(int dtype, int64_t n, const double *alpha, const void *x,
+              void *y, int conj, void *stream);
+
+/* y = alpha*x + beta*y.  Replaces Tensor.__add__ (tensor.py:125-140). */
+int tnc_axpby(int dtype, int64_t n, const double *alpha, const void *x,
+              const double *beta, void *y, void *stream);
+
+/* dtype conversion (real -> complex sets im = 0; complex -> real drops im). */
+int tnc_cast(int src_dtype, int dst_dtype, int64_t n, const void *src,
+             void *dst, void *stream);
+
+/* out[0] = sqrt(sum |x_i|^2), accumulated in double, into a device double.
+ * Replaces np.linalg.norm (tensor.py:587-590, onedim_core.py:279, 655-658). */
+int tnc_nrm2(int dtype, int64_t n, const void *x, double *out, void *stream);
+
+/* out[0..1] = sum op(x_i) y_i as (re, im) in double (device).  Used for the
+ * scalar closing of inner_product_mps (onedim_core.py:1666-1683). */
+int tnc_dot(int dtype, int64_t n, const void *x, const void *y, int conj_x,
+            double *out, void *stream);
+
+/* Trace over axes (axis1, axis2) of a dense tensor; dst holds the remaining
+ * axes in order.  Replaces np.trace in Tensor.contract_internal
+ * (tensor.py:318-334). */
+int tnc_trace(int dtype, int rank, const int64_t *shape, int axis1, int axis2,
+              const void *src, void *dst, void *stream);
+
+/* A[i, :] *= f(d[i]) for a rows x cols row-major A (lda), d real (float for
+ * F32/C64, double for F64/C128), f = identity (mode 0) or sqrt (mode 1).
+ * Replaces the dense diag(S) contractions that absorb singular values
+ * (tensor.py:940-959, 1166-1182; onedim_core.py:347-351). */
+int tnc_scale_rows(int dtype, int64_t rows, int64_t cols, const void *d,
+                   int mode, void *A, int64_t lda, void *stream);
+/* A[:, j] *= f(d[j]); same conventions. */
+int tnc_scale_cols(int dtype, int64_t rows, int64_t cols, const void *d,
+                   int mode, void *A, int64_t lda, void *stream);
+
+/* dst[i, j] = src[i, j] for a rows x cols block with leading dimensions
+ * lds / ldd.  The slicing copies of truncation, U.data[:, :, :k]
+ * (onedim_core.py:340-343, tensor.py:1158-1163), and zero padding
+ * (Tensor.pad_index, tensor.py:543-563). */
+int tnc_copy2d(int dtype, int64_t rows, int64_t cols, const void *src,
+               int64_t lds, void *dst, int64_t ldd, void *stream);
+
+/* out = diag(d) as a dense n x n matrix (d real, see tnc_scale_rows).  The
+ * S tensor of tensor_svd, np.diag(s) (tensor.py:940). */
+int tnc_diag_matrix(int dtype, int64_t n, const void *d, void *out, void *stream);
+
+/* ------------------------------------------------------------ contraction */
+
+/* Batched GEMM on row-major operands:
+ *   C_b = alpha * op(A_b) * op(B_b) + beta * C_b,  b < batch,
+ * op(A_b) is m x k, op(B_b) is k x n, X_b = X + b*strideX.  This is the
+ * product np.tensordot performs after matricising both operands
+ * (tensor.py:735); the label -> axis resolution stays on the host. */
+int tnc_gemm(int dtype, int opA, int opB, int64_t m, int64_t n, int64_t k,
+             const double *alpha, const void *A, int64_t lda, int64_t strideA,
+             const void *B, int64_t ldb, int64_t strideB, const double *beta,
+             void *C, int64_t ldc, int64_t strideC, int64_t batch,
+             void *stream);
+
+/* One MPO-MPS site product with the reference's fused bond layout
+ * (contract_mps_mpo, onedim_core.py:1702-1704: contract over phys/physin
+ * then consolidate_indices, fused bond = a*D + b):
+ *   out[l*Dl + wl][po][r*Dr + wr]      (layout 0: (left, physout, right),
+ *                                        the reference's label order)
+ *   out[po][l*Dl + wl][r*Dr + wr]      (layout 1: (phys, left, right))
+ *   = sum_p A[p][l][r] * W[po][p][wl][wr].
+ * A is (d_in, chl, chr), W is (d_out, d_in, Dl, Dr). */
+int tnc_mps_mpo_site(int dtype, int64_t d_in, int64_t d_out, int64_t chl,
+                     int64_t chr, int64_t Dl, int64_t Dr, const void *A,
+                     const void *W, void *out, int layout, void *stream);
+
+/* ------------------------------------------------------------ factorisations */
+
+/* Reduced QR of a row-major m x n matrix A (lda): Q is m x k (ldq = k),
+ * R is k x n (ldr = n), k = min(m, n).  Householder reflectors in LAPACK's
+ * convention (geqrf + ungqr), factored by one cooperative persistent launch
+ * as a column-owner dataflow, Q formed explicitly.  info (device int):
+ * TNC_OK or TNC_ERR_TIMEOUT.
+ * Replaces np.linalg.qr(mode="reduced") in tensor_qr (tensor.py:1044). */
+int tnc_qr_workspace_size(int dtype, int64_t m, int64_t n, size_t *bytes);
+int tnc_qr(int dtype, int64_t m, int64_t n, const void *A, int64_t lda,
+           void *Q, void *R, void *work, size_t work_bytes, int *info,
+           void *stream);
+
+/* Thin SVD of a row-major m x n matrix A (lda): U is m x k, S has k real
+ * values sorted descending (float for F32/C64, double for F64/C128), VH is
+ * k x n, k = min(m, n).  One-sided (Hestenes) Jacobi with a round-robin
+ * ordering, run by one persistent cooperative launch.  max_sweeps <= 0
+ * selects 40; tol <= 0 selects sqrt(max(m,n)) * eps.  info (device, 4 ints):
+ * [0] status (TNC_OK / TNC_ERR_NOT_CONVERGED / TNC_ERR_NONFINITE /
+ * TNC_ERR_TIMEOUT), [1] sweeps used, [2] rotations in the last sweep.
+ * Replaces np.linalg.svd(full_matrices=False) in tensor_svd (tensor.py:915)
+ * and its scipy gesvd retry (tensor.py:916-929). */
+int tnc_svd_workspace_size(int dtype, int64_t m, int64_t n, size_t *bytes);
+int tnc_svd(int dtype, int64_t m, int64_t n, const void *A, int64_t lda,
+            void *U, void *S, void *VH, int max_sweeps, double tol,
+            void *work, size_t work_bytes, int *info, void *stream);
+
+/* Truncation decision on descending singular values S (n, real type of
+ * dtype): k = #{ s_i > t } capped at chi (chi <= 0: no cap), t = threshold
+ * (relative = 0) or threshold * S[0] (relative = 1).  Writes k (device
+ * int64) and the discarded weight sum_{i >= k} s_i^2 (device double).  The
+ * rule of truncated_svd (tensor.py:1137-1152) and of left_canonise
+ * (onedim_core.py:332-339; s/s_max > threshold is s > threshold*s_max). */
+int tnc_truncation_rank(int dtype, int64_t n, const void *S, int64_t chi,
+                        double threshold, int relative, int64_t *k,
+                        double *discarded, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TNCONTRACT_GB300_H */

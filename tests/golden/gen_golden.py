@@ -1,0 +1,273 @@
+"""Generate the golden fixtures in this folder by running the reference
+library (andrewdarmawan/tncontract, pure Python on NumPy/SciPy) itself.
+
+Run from the repository root with the reference checkout importable:
+
+    python tests/golden/gen_golden.py /path/to/tncontract-checkout
+
+The reference predates NumPy 2; two aliases it uses (``np.product``,
+``np.float``) are restored at run time before it is imported.  The checkout is
+only read.  Outputs (small ``.npz`` / ``.json`` files) are committed and are
+what the tests compare against; the tests never import the reference.
+
+Inputs are regenerated from seeds by ``oracle/tn_oracle.py``'s generators
+(``numpy.random.default_rng``), except the reference's own pickled 10-site
+test MPS, whose arrays are stored here verbatim.
+"""
+import json
+import os
+import pickle
+import sys
+import time
+
+import numpy as np
+
+if not hasattr(np, "product"):
+    np.product = np.prod
+if not hasattr(np, "float"):
+    np.float = float
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.dont_write_bytecode = True
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import tn_oracle as O  # noqa: E402
+
+
+def _ref(path):
+    sys.path.insert(0, path)
+    import tncontract as tn  # noqa
+    return tn
+
+
+def to_sites(mps, tn):
+    """Reference MPS -> list of (phys,left,right) arrays (label-aware)."""
+    out = []
+    for t in mps:
+        lab = list(t.labels)
+        perm = [lab.index(mps.phys_label), lab.index(mps.left_label),
+                lab.index(mps.right_label)]
+        out.append(np.ascontiguousarray(np.transpose(t.data, perm)))
+    return out
+
+
+def spectra_of(sites):
+    return [np.asarray(s) for s in O.bond_spectra(sites)]
+
+
+def pack_list(prefix, arrs, store):
+    store[prefix + "_n"] = np.array(len(arrs))
+    for i, a in enumerate(arrs):
+        store["%s_%d" % (prefix, i)] = np.asarray(a)
+
+
+def gen_label_cases(tn, store, meta):
+    rng = np.random.default_rng(11)
+    # README / docstring label cases (tensor.py:659-683, README.md:37-128)
+    A = tn.Tensor(rng.random((2, 2)), labels=["spam", "eggs"])
+    B = tn.Tensor(rng.random((2, 3, 2, 4)))
+    store["lc_A"] = A.data
+    store["lc_B"] = B.data
+    C = tn.contract(A, B, "spam", "i2")
+    D = tn.contract(A, B, ["spam", "eggs"], ["i0", "i2"])
+    E = A["spam", "eggs"] * B["i0", "i2"]
+    store["lc_C"] = C.data
+    store["lc_D"] = D.data
+    store["lc_E"] = E.data
+    meta["lc_C_labels"] = C.labels
+    meta["lc_D_labels"] = D.labels
+    meta["lc_E_labels"] = E.labels
+    # duplicate labels and index_slice (tensor.py:702-731)
+    T1 = tn.Tensor(rng.random((2, 3, 2, 4)), labels=["a", "b", "a", "c"])
+    T2 = tn.Tensor(rng.random((2, 5, 2)), labels=["x", "y", "x"])
+    store["lc_T1"] = T1.data
+    store["lc_T2"] = T2.data
+    F = tn.contract(T1, T2, "a", "x")
+    G = tn.contract(T1, T2, "a", "x", index_slice1=[-1], index_slice2=[0])
+    store["lc_F"] = F.data
+    store["lc_G"] = G.data
+    meta["lc_F_labels"] = F.labels
+    meta["lc_G_labels"] = G.labels
+    # consolidate_indices (tensor.py:340-370)
+    H = tn.Tensor(rng.random((2, 3, 4, 5)), labels=["z", "b", "z", "a"])
+    store["lc_H"] = H.data
+    H2 = H.copy()
+    H2.consolidate_indices()
+    store["lc_Hc"] = H2.data
+    meta["lc_Hc_labels"] = H2.labels
+    # tensor product and con (tncon.py:4-159)
+    P = tn.tensor_product(A, tn.Tensor(rng.random(3), labels=["q"]))
+    store["lc_P"] = P.data
+    meta["lc_P_labels"] = P.labels
+    # con docstring-style ring: A_i labelled left_i/right_i, periodic trace
+    R = tn.Tensor(rng.random((2, 2)), labels=["left", "right"])
+    store["lc_R"] = R.data
+    tl = [R.suf(str(i)) for i in range(5)]
+    pairs = [("right" + str(j), "left" + str(j + 1)) for j in range(4)]
+    ring = tn.con(tl, pairs, ("right4", "left0"))
+    store["lc_ring"] = np.asarray(ring.data)
+    meta["lc_ring_labels"] = ring.labels
+    # con with a multi-edge pair, an internal trace and a disconnected tensor
+    X = tn.Tensor(rng.random((2, 3, 4)), labels=["x1", "x2", "x3"])
+    Y = tn.Tensor(rng.random((3, 4, 5)), labels=["y1", "y2", "y3"])
+    Z = tn.Tensor(rng.random((6, 6, 2)), labels=["z1", "z2", "z3"])
+    W = tn.Tensor(rng.random(7), labels=["w1"])
+    store["lc_X"], store["lc_Y"], store["lc_Z"], store["lc_W"] = X.data, Y.data, Z.data, W.data
+    K = tn.con(X, Y, Z, W, ("x2", "y1"), ("x3", "y2"), ("z1", "z2"), ("x1", "z3"))
+    store["lc_K"] = np.asarray(K.data)
+    meta["lc_K_labels"] = K.labels
+    # tensor_svd / truncated_svd / tensor_qr / tensor_lq labels & shapes
+    S0 = tn.Tensor(rng.random((2, 3, 4)), labels=["i0", "i1", "i2"])
+    store["lc_S0"] = S0.data
+    U, S, V = tn.tensor_svd(S0, ["i0", "i2"])
+    meta["svd_labels"] = [U.labels, S.labels, V.labels]
+    meta["svd_shapes"] = [list(U.shape), list(S.shape), list(V.shape)]
+    store["svd_s"] = np.diag(S.data)
+    U2, V2, tr = tn.truncated_svd(S0, ["i0", "i2"], chi=2)
+    meta["tsvd_labels"] = [U2.labels, V2.labels]
+    meta["tsvd_shapes"] = [list(U2.shape), list(V2.shape)]
+    store["tsvd_trunc"] = np.asarray(tr)
+    U3, V3, tr3 = tn.truncated_svd(S0, ["i0", "i2"], chi=0, threshold=0.3,
+                                   absolute=False, absorb_singular_values="both")
+    meta["tsvd_rel_shapes"] = [list(U3.shape), list(V3.shape)]
+    store["tsvd_rel_trunc"] = np.asarray(tr3)
+    Q, Rr = tn.tensor.tensor_qr(S0, ["i0", "i2"])
+    meta["qr_labels"] = [Q.labels, Rr.labels]
+    meta["qr_shapes"] = [list(Q.shape), list(Rr.shape)]
+    L, Q2 = tn.tensor.tensor_lq(S0, ["i0", "i2"])
+    meta["lq_labels"] = [L.labels, Q2.labels]
+    meta["lq_shapes"] = [list(L.shape), list(Q2.shape)]
+
+
+def gen_fixture_10site(tn, ref_path, store, meta):
+    """The reference's own test MPS (tests/random_10site_mps.dat) and what its
+    tests pin (test_canonical_form_mps_conversion.py:31-80)."""
+    with open(os.path.join(ref_path, "tncontract/tests/random_10site_mps.dat"), "rb") as f:
+        psi = pickle.load(f, encoding="latin1")
+    meta["fx_labels"] = [list(t.labels) for t in psi]
+    meta["fx_mps_labels"] = [psi.left_label, psi.right_label, psi.phys_label]
+    sites = to_sites(psi, tn)
+    pack_list("fx_site", sites, store)
+    store["fx_norm"] = np.array(psi.norm())
+    a = psi.copy()
+    a.svd_compress(threshold=1e-12, normalise=False)
+    store["fx_c_norm"] = np.array(a.norm())
+    meta["fx_c_bonds"] = [int(x) for x in a.bonddims()]
+    meta["fx_c_labels"] = [list(t.labels) for t in a]
+    pack_list("fx_c_spectra", spectra_of(to_sites(a, tn)), store)
+    b = psi.copy()
+    b.svd_compress(threshold=1e-12, normalise=True)
+    store["fx_cn_norm"] = np.array(b.norm())
+    c = psi.copy()
+    c.left_canonise()
+    meta["fx_lc_bonds"] = [int(x) for x in c.bonddims()]
+    meta["fx_lc_canon"] = list(c.check_canonical_form(threshold=1e-10, print_output=False))
+    store["fx_ip"] = np.array(tn.onedim.inner_product_mps(psi, c))
+
+
+def gen_config1(tn, store, meta):
+    """Config: N=32, d=2, chi=32 float64 seed 0; left_canonical_form_mps then
+    svd_compress(chi=16)."""
+    sites = O.random_mps(0, 32, 2, 32, np.float64)
+    mps = tn.onedim.MatrixProductState(
+        [tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+    t0 = time.perf_counter()
+    lc = tn.onedim.left_canonical_form_mps(mps)
+    comp = lc.copy()
+    comp.svd_compress(chi=16)
+    meta["c1_ref_seconds"] = time.perf_counter() - t0
+    meta["c1_lc_bonds"] = [int(x) for x in lc.bonddims()]
+    meta["c1_c_bonds"] = [int(x) for x in comp.bonddims()]
+    meta["c1_c_labels"] = [list(t.labels) for t in comp][:3]
+    cs = to_sites(comp, tn)
+    store["c1_norm_in"] = np.array(mps.norm())
+    store["c1_norm_lc"] = np.array(lc.norm())
+    store["c1_norm_c"] = np.array(comp.norm())
+    ip = tn.onedim.inner_product_mps
+    store["c1_fid_vs_input"] = np.array(abs(ip(mps, comp)) ** 2 /
+                                        (ip(mps, mps) * ip(comp, comp)))
+    pack_list("c1_c_spectra", spectra_of(cs), store)
+
+
+def gen_config2(tn, store, meta, N, chi, tag):
+    """TFIM (D=3) MPO applied to a normalised random complex128 MPS, then
+    svd_compress(chi) (method) and svd_compress_mps(chi) (function)."""
+    sites = O.random_mps(0, N, 2, chi, np.complex128, normalise=True)
+    mpo = O.tfim_mpo(N)
+    mps = tn.onedim.MatrixProductState(
+        [tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+    W = tn.onedim.MatrixProductOperator(
+        [tn.Tensor(w, ["physout", "physin", "left", "right"]) for w in mpo])
+    t0 = time.perf_counter()
+    phi = tn.onedim.contract_mps_mpo(mps, W)
+    t1 = time.perf_counter()
+    m = phi.copy()
+    m.svd_compress(chi=chi)
+    t2 = time.perf_counter()
+    meta[tag + "_ref_seconds_apply"] = t1 - t0
+    meta[tag + "_ref_seconds_method"] = t2 - t1
+    meta[tag + "_phi_labels"] = list(phi[1].labels)
+    meta[tag + "_phi_shape"] = list(phi[1].shape)
+    meta[tag + "_phi_phys"] = phi.phys_label
+    if N <= 16:
+        store[tag + "_phi_site1"] = phi[1].data
+    meta[tag + "_m_bonds"] = [int(x) for x in m.bonddims()]
+    meta[tag + "_m_labels"] = [list(t.labels) for t in m][:3]
+    ip = tn.onedim.inner_product_mps
+    store[tag + "_norm_phi"] = np.array(phi.norm())
+    store[tag + "_norm_m"] = np.array(m.norm())
+    store[tag + "_fid_m_phi"] = np.array(abs(ip(phi, m)) ** 2 / (ip(phi, phi) * ip(m, m)))
+    ms = to_sites(m, tn)
+    pack_list(tag + "_m_spectra", spectra_of(ms), store)
+    if N <= 16:
+        f = tn.onedim.svd_compress_mps(phi, chi)
+        meta[tag + "_f_bonds"] = [int(x) for x in f.bonddims()]
+        store[tag + "_norm_f"] = np.array(f.norm())
+        store[tag + "_fid_f_m"] = np.array(abs(ip(f, m)) ** 2 / (ip(f, f) * ip(m, m)))
+        pack_list(tag + "_f_spectra", spectra_of(to_sites(f, tn)), store)
+
+
+def gen_peps(tn, store, meta, L, D, d, chi, tag, seed=2):
+    rows = O.random_peps(seed, L, L, D, d)
+    peps = tn.twodim.SquareLatticePEPS(
+        [[tn.Tensor(a, ["phys", "up", "right", "down", "left"]) for a in r] for r in rows])
+    t0 = time.perf_counter()
+    v = tn.twodim.inner_product_peps(peps, peps, exact_contract=False, chi=chi)
+    meta[tag + "_ref_seconds"] = time.perf_counter() - t0
+    val = v.data if hasattr(v, "data") else v
+    val = np.longdouble(np.real(val))
+    m, e = np.frexp(np.float64(val / np.longdouble(10.0) ** int(np.floor(np.log10(float(val))))))
+    meta[tag + "_value_str"] = repr(val)
+    meta[tag + "_log10"] = float(np.log10(val))
+    store[tag + "_value"] = np.array(float(val))
+    if L <= 4:
+        ex = tn.twodim.inner_product_peps(peps, peps, exact_contract=True)
+        store[tag + "_exact"] = np.array(float(np.real(ex.data)))
+
+
+def main():
+    ref_path = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    tn = _ref(ref_path)
+    store, meta = {}, {}
+    gen_label_cases(tn, store, meta)
+    gen_fixture_10site(tn, ref_path, store, meta)
+    np.savez_compressed(os.path.join(HERE, "labels_and_fixture.npz"), **store)
+    with open(os.path.join(HERE, "labels_and_fixture.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    for fn, job in [("config1", lambda s, m: gen_config1(tn, s, m)),
+                    ("config2_small", lambda s, m: gen_config2(tn, s, m, 12, 16, "c2s")),
+                    ("config2_chi128", lambda s, m: gen_config2(tn, s, m, 64, 128, "c2")),
+                    ("peps", lambda s, m: (gen_peps(tn, s, m, 4, 2, 2, 4, "p4"),
+                                           gen_peps(tn, s, m, 8, 4, 2, 16, "p8c16"),
+                                           gen_peps(tn, s, m, 8, 4, 2, 64, "p8c64")))]:
+        s, m = {}, {}
+        t = time.perf_counter()
+        job(s, m)
+        print(fn, "%.1fs" % (time.perf_counter() - t), flush=True)
+        np.savez_compressed(os.path.join(HERE, fn + ".npz"), **s)
+        with open(os.path.join(HERE, fn + ".json"), "w") as f:
+            json.dump(m, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

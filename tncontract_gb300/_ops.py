@@ -1,0 +1,405 @@
+"""Device operations on CUDA ``torch.Tensor`` storage, each one call into the
+native C ABI (``include/tncontract_gb300.h``).
+
+PyTorch provides device memory and the current stream only; every
+arithmetic / data-movement step of the hot path runs in the library's own
+sm_103a kernels.  All tensors handled here are dense and C-contiguous.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+_CODE = {torch.float32: L.F32, torch.float64: L.F64,
+         torch.complex64: L.C64, torch.complex128: L.C128}
+_REAL = {torch.float32: torch.float32, torch.float64: torch.float64,
+         torch.complex64: torch.float32, torch.complex128: torch.float64}
+_NP2TORCH = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+             np.dtype(np.complex64): torch.complex64, np.dtype(np.complex128): torch.complex128}
+
+
+class LinAlgError(np.linalg.LinAlgError):
+    pass
+
+
+def device():
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def code(dtype):
+    try:
+        return _CODE[dtype]
+    except KeyError:
+        raise TypeError("unsupported dtype %s (float32/float64/complex64/complex128)" % dtype)
+
+
+def real_dtype(dtype):
+    return _REAL[dtype]
+
+
+def is_complex(dtype):
+    return dtype in (torch.complex64, torch.complex128)
+
+
+def _pair(x):
+    z = complex(x)
+    return (C.c_double * 2)(z.real, z.imag)
+
+
+def _arr(ctype, seq):
+    seq = list(seq)
+    return (ctype * max(1, len(seq)))(*seq)
+
+
+def _call(name, *args):
+    L.check(name, getattr(L.lib(), name)(*args))
+
+
+def empty(shape, dtype):
+    return torch.empty(tuple(int(s) for s in shape), dtype=dtype, device=device())
+
+
+def zeros(shape, dtype):
+    # a zero fill is allocation plumbing (a memset), not hot-path arithmetic
+    return torch.zeros(tuple(int(s) for s in shape), dtype=dtype, device=device())
+
+
+_WS = {}
+
+
+def workspace(nbytes):
+    """Per-stream reusable workspace (stream ordering makes reuse safe)."""
+    key = (torch.cuda.current_device(), torch.cuda.current_stream().cuda_stream)
+    buf = _WS.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 1 << 20), dtype=torch.uint8, device=device())
+        _WS[key] = buf
+    return buf
+
+
+# ------------------------------------------------------------------ creation
+
+
+def to_device(x, dtype=None):
+    """Copy array-like ``x`` to a new contiguous device tensor.  Integer and
+    boolean inputs become float64 (the engine computes in floating point)."""
+    if isinstance(x, torch.Tensor):
+        t = x
+        if dtype is not None and t.dtype != dtype:
+            t = t.to(dtype)
+        if t.dtype not in _CODE:
+            t = t.to(torch.complex128 if t.is_complex() else torch.float64)
+        if t.device.type != "cuda" or t.device.index != torch.cuda.current_device():
+            return t.contiguous().to(device())
+        return t.contiguous().clone()
+    a = np.asarray(x)
+    if a.dtype not in _NP2TORCH:
+        a = a.astype(np.complex128 if np.iscomplexobj(a) else np.float64)
+    if dtype is not None:
+        a = a.astype({v: k for k, v in _NP2TORCH.items()}[dtype])
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device())
+
+
+def copy(t):
+    return t.clone()
+
+
+# ------------------------------------------------------------------ movement
+
+
+def permute(x, perm, conj=False):
+    """Return transpose(x, perm) (optionally conjugated) as a new tensor;
+    ``x`` itself when the permutation is the identity and no conj is asked."""
+    perm = [int(p) for p in perm]
+    conj = bool(conj) and is_complex(x.dtype)
+    if perm == list(range(x.dim())) and not conj:
+        return x
+    x = x.contiguous()
+    shape = [x.shape[p] for p in perm]
+    moving = [p for p in perm if x.shape[p] != 1]
+    if not conj and moving == sorted(moving):
+        return x.reshape(shape)  # only unit axes move: a view suffices
+    out = empty(shape, x.dtype)
+    if out.numel() == 0:
+        return out
+    _call("tnc_permute", code(x.dtype), _p(x), _p(out), x.dim(),
+          _arr(C.c_int64, x.shape), _arr(C.c_int, perm), int(conj), _stream())
+    return out
+
+
+def rollaxis(x, axis, start):
+    """np.rollaxis semantics (used by the reference's axis moves)."""
+    n = x.dim()
+    axis = axis % n if n else 0
+    if start < 0:
+        start += n
+    order = list(range(n))
+    order.remove(axis)
+    if start > axis:
+        start -= 1
+    order.insert(start, axis)
+    return permute(x, order)
+
+
+def cast(x, dtype):
+    if x.dtype == dtype:
+        return x
+    out = empty(x.shape, dtype)
+    if x.numel():
+        _call("tnc_cast", code(x.dtype), code(dtype), x.numel(), _p(x.contiguous()), _p(out), _stream())
+    return out
+
+
+def scale(x, alpha, conj=False, out=None):
+    x = x.contiguous()
+    if out is None:
+        out = empty(x.shape, x.dtype)
+    if x.numel():
+        _call("tnc_scale", code(x.dtype), x.numel(), _pair(alpha), _p(x), _p(out),
+              int(bool(conj) and is_complex(x.dtype)), _stream())
+    return out
+
+
+def conj(x):
+    if not is_complex(x.dtype):
+        return x
+    return scale(x, 1.0, conj=True)
+
+
+def axpby(alpha, x, beta, y):
+    """y <- alpha x + beta y (in place on y)."""
+    if x.numel():
+        _call("tnc_axpby", code(x.dtype), x.numel(), _pair(alpha), _p(x.contiguous()),
+              _pair(beta), _p(y), _stream())
+    return y
+
+
+def add(x, y):
+    out = y.clone()
+    return axpby(1.0, x, 1.0, out)
+
+
+def copy2d(src, rows, cols, lds, dst, ldd, src_off=0, dst_off=0):
+    """dst[i, j] = src[i, j] for a rows x cols block (element offsets)."""
+    if rows * cols:
+        es = src.element_size()
+        _call("tnc_copy2d", code(src.dtype), rows, cols, C.c_void_p(src.data_ptr() + src_off * es),
+              lds, C.c_void_p(dst.data_ptr() + dst_off * es), ldd, _stream())
+    return dst
+
+
+def slice_last(data, k):
+    """Contiguous copy of data[..., :k] (``data`` itself when k is the full extent)."""
+    n = data.shape[-1]
+    if k == n:
+        return data
+    rows = data.numel() // n if n else 0
+    out = empty(tuple(data.shape[:-1]) + (k,), data.dtype)
+    copy2d(data.contiguous(), rows, k, n, out, k)
+    return out
+
+
+def diag_matrix(s, dtype):
+    n = s.shape[0]
+    out = empty((n, n), dtype)
+    if n:
+        _call("tnc_diag_matrix", code(dtype), n, _p(s.contiguous()), _p(out), _stream())
+    return out
+
+
+def scale_rows(A, d, mode=0):
+    """A[i, :] *= d[i] (mode 0) or sqrt(d[i]) (mode 1), in place; A 2-D."""
+    r, c = A.shape
+    if r * c:
+        _call("tnc_scale_rows", code(A.dtype), r, c, _p(d.contiguous()), int(mode), _p(A), c, _stream())
+    return A
+
+
+def scale_cols(A, d, mode=0):
+    r, c = A.shape
+    if r * c:
+        _call("tnc_scale_cols", code(A.dtype), r, c, _p(d.contiguous()), int(mode), _p(A), c, _stream())
+    return A
+
+
+def trace(x, a1, a2):
+    x = x.contiguous()
+    out = empty([s for i, s in enumerate(x.shape) if i not in (a1, a2)], x.dtype)
+    if out.numel():
+        _call("tnc_trace", code(x.dtype), x.dim(), _arr(C.c_int64, x.shape), int(a1), int(a2),
+              _p(x), _p(out), _stream())
+    return out
+
+
+# ------------------------------------------------------------------ reductions
+
+
+def nrm2_device(x):
+    out = torch.empty(1, dtype=torch.float64, device=device())
+    _call("tnc_nrm2", code(x.dtype), x.numel(), _p(x.contiguous()), _p(out), _stream())
+    return out
+
+
+def nrm2(x):
+    """Frobenius norm as a Python float (synchronises)."""
+    return float(nrm2_device(x).item())
+
+
+def dot_device(x, y, conj_x=False):
+    out = torch.empty(2, dtype=torch.float64, device=device())
+    _call("tnc_dot", code(x.dtype), x.numel(), _p(x.contiguous()), _p(y.contiguous()),
+          int(bool(conj_x)), _p(out), _stream())
+    return out
+
+
+# ------------------------------------------------------------------ contraction
+
+
+def gemm(opA, opB, m, n, k, A, lda, B, ldb, Cm, ldc, alpha=1.0, beta=0.0,
+         batch=1, sA=0, sB=0, sC=0):
+    _call("tnc_gemm", code(Cm.dtype), opA, opB, m, n, k, _pair(alpha), _p(A), lda, sA,
+          _p(B), ldb, sB, _pair(beta), _p(Cm), ldc, sC, batch, _stream())
+    return Cm
+
+
+def matmul(a, b, opA=L.OP_N, opB=L.OP_N, out=None):
+    """out = op(a) @ op(b) for 2-D tensors."""
+    m = a.shape[1] if opA in (L.OP_T, L.OP_C) else a.shape[0]
+    k = a.shape[0] if opA in (L.OP_T, L.OP_C) else a.shape[1]
+    n = b.shape[0] if opB in (L.OP_T, L.OP_C) else b.shape[1]
+    if out is None:
+        out = empty((m, n), a.dtype)
+    if m * n:
+        gemm(opA, opB, m, n, k, a.contiguous(), a.shape[1], b.contiguous(), b.shape[1], out, n)
+    return out
+
+
+def tensordot(a, b, axes_a, axes_b):
+    """np.tensordot(a, b, (axes_a, axes_b)) on device: at most one permute per
+    operand (none when the contracted axes are already leading or trailing),
+    then one GEMM."""
+    axes_a = [int(x) % a.dim() for x in axes_a] if a.dim() else []
+    axes_b = [int(x) % b.dim() for x in axes_b] if b.dim() else []
+    dt = torch.promote_types(a.dtype, b.dtype)
+    a = cast(a.contiguous(), dt)
+    b = cast(b.contiguous(), dt)
+    free_a = [i for i in range(a.dim()) if i not in axes_a]
+    free_b = [i for i in range(b.dim()) if i not in axes_b]
+    ma = int(np.prod([a.shape[i] for i in free_a], dtype=np.int64))
+    nb = int(np.prod([b.shape[i] for i in free_b], dtype=np.int64))
+    kk = int(np.prod([a.shape[i] for i in axes_a], dtype=np.int64))
+    out = empty([a.shape[i] for i in free_a] + [b.shape[i] for i in free_b], dt)
+    if ma == 0 or nb == 0:
+        return out
+    if free_a + axes_a == list(range(a.dim())):
+        opA, Am, lda = L.OP_N, a, kk
+    elif axes_a + free_a == list(range(a.dim())):
+        opA, Am, lda = L.OP_T, a, ma
+    else:
+        opA, Am, lda = L.OP_N, permute(a, free_a + axes_a), kk
+    if axes_b + free_b == list(range(b.dim())):
+        opB, Bm, ldb = L.OP_N, b, nb
+    elif free_b + axes_b == list(range(b.dim())):
+        opB, Bm, ldb = L.OP_T, b, kk
+    else:
+        opB, Bm, ldb = L.OP_N, permute(b, axes_b + free_b), nb
+    gemm(opA, opB, ma, nb, kk, Am, max(lda, 1), Bm, max(ldb, 1), out, nb)
+    return out
+
+
+def mps_mpo_site(A, W, layout):
+    """Fused MPO-MPS site product; A (din, chl, chr), W (dout, din, Dl, Dr)."""
+    din, chl, chr_ = A.shape
+    dout, din2, Dl, Dr = W.shape
+    assert din == din2
+    dt = torch.promote_types(A.dtype, W.dtype)
+    A = cast(A.contiguous(), dt)
+    W = cast(W.contiguous(), dt)
+    shape = (chl * Dl, dout, chr_ * Dr) if layout == 0 else (dout, chl * Dl, chr_ * Dr)
+    out = empty(shape, dt)
+    _call("tnc_mps_mpo_site", code(dt), din, dout, chl, chr_, Dl, Dr, _p(A), _p(W), _p(out),
+          int(layout), _stream())
+    return out
+
+
+# ------------------------------------------------------------------ factorisations
+
+
+def svd(M, max_sweeps=0, tol=0.0, check=True, info_out=None):
+    """Thin SVD of a 2-D device matrix: (U, S, VH), S real descending.
+    Raises LinAlgError on non-convergence and ValueError on non-finite input,
+    like np.linalg.svd / scipy gesvd."""
+    M = M.contiguous()
+    m, n = M.shape
+    k = min(m, n)
+    dt = M.dtype
+    U = empty((m, k), dt)
+    S = empty((k,), real_dtype(dt))
+    VH = empty((k, n), dt)
+    if k == 0:
+        return U, S, VH
+    sz = C.c_size_t()
+    _call("tnc_svd_workspace_size", code(dt), m, n, C.byref(sz))
+    ws = workspace(sz.value)
+    info = torch.empty(4, dtype=torch.int32, device=device())
+    _call("tnc_svd", code(dt), m, n, _p(M), n, _p(U), _p(S), _p(VH), int(max_sweeps), float(tol),
+          _p(ws), sz.value, _p(info), _stream())
+    if info_out is not None:
+        info_out.append(info)
+    if check:
+        st = int(info[0].item())
+        if st == L.ERR_NONFINITE:
+            raise ValueError("array must not contain infs or NaNs")
+        if st == L.ERR_NOT_CONVERGED:
+            raise LinAlgError("SVD did not converge")
+        if st != L.OK:
+            raise L.NativeError("tnc_svd", st)
+    return U, S, VH
+
+
+def qr(M, check=True):
+    """Reduced QR of a 2-D device matrix: (Q, R)."""
+    M = M.contiguous()
+    m, n = M.shape
+    k = min(m, n)
+    Q = empty((m, k), M.dtype)
+    R = empty((k, n), M.dtype)
+    if k == 0:
+        return Q, R
+    sz = C.c_size_t()
+    _call("tnc_qr_workspace_size", code(M.dtype), m, n, C.byref(sz))
+    ws = workspace(sz.value)
+    info = torch.empty(1, dtype=torch.int32, device=device())
+    _call("tnc_qr", code(M.dtype), m, n, _p(M), n, _p(Q), _p(R), _p(ws), sz.value, _p(info), _stream())
+    if check:
+        st = int(info.item())
+        if st != L.OK:
+            raise L.NativeError("tnc_qr", st)
+    return Q, R
+
+
+def truncation_rank(S, chi, threshold, relative):
+    """(k, discarded weight) for descending singular values S (synchronises)."""
+    buf = torch.empty(2, dtype=torch.float64, device=device())
+    kbuf = buf[0:1].view(torch.int64)
+    _call("tnc_truncation_rank", code(S.dtype), S.numel(), _p(S), int(chi or 0), float(threshold),
+          int(bool(relative)), _p(kbuf), C.c_void_p(buf.data_ptr() + 8), _stream())
+    h = buf.cpu()
+    return int(h[0:1].view(torch.int64).item()), float(h[1].item())
+
+
+def prod(shape):
+    return int(math.prod(int(s) for s in shape))

@@ -1,0 +1,108 @@
+// Helpers for the persistent (cooperatively launched) factorisation kernels:
+// a grid barrier and flag waits whose spins are bounded.  A wait that gives
+// up records TNC_ERR_TIMEOUT in the shared error word and returns false; all
+// CTAs then leave the kernel at their next wait, so no launch can hang.
+#pragma once
+#include "tnc_common.cuh"
+
+namespace tnc {
+
+// Roughly 2-4 s of polling at ~150 ns per iteration: orders of magnitude above
+// any legitimate wait (one Jacobi round or one Householder column step).
+constexpr long long kSpinLimit = 1LL << 24;
+
+struct SyncWords {
+  unsigned count;  // arrivals at the current barrier
+  unsigned gen;    // barrier generation
+  int err;         // first error recorded by any CTA (0 = none)
+  int pad;
+};
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(volatile const int*)p; }
+__device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(volatile const unsigned*)p; }
+
+// All CTAs of the grid; returns false if any CTA recorded an error.
+__device__ __forceinline__ bool grid_barrier(SyncWords* sw, unsigned nblocks) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned g = ld_volatile(&sw->gen);
+    __threadfence();
+    unsigned prev = atomicAdd(&sw->count, 1u);
+    if (prev == nblocks - 1) {
+      atomicExch(&sw->count, 0u);
+      __threadfence();
+      atomicAdd(&sw->gen, 1u);
+    } else {
+      long long spins = 0;
+      while (ld_volatile(&sw->gen) == g) {
+        if (ld_volatile(&sw->err)) { ok = 0; break; }
+        if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (ld_volatile(&sw->err)) ok = 0;
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// One warp waits until *flag != 0; returns false on error / timeout.
+__device__ __forceinline__ bool warp_wait_flag(const int* flag, SyncWords* sw) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) {
+    long long spins = 0;
+    while (ld_volatile(flag) == 0) {
+      if (ld_volatile(&sw->err)) { ok = 0; break; }
+      if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
+      __nanosleep(32);
+    }
+    __threadfence();
+  }
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+
+// L2-only loads/stores for data other CTAs write during the same launch.
+template <typename T> __device__ __forceinline__ T ldcg(const T* p);
+template <> __device__ __forceinline__ float ldcg<float>(const float* p) { return __ldcg(p); }
+template <> __device__ __forceinline__ double ldcg<double>(const double* p) { return __ldcg(p); }
+template <> __device__ __forceinline__ c64 ldcg<c64>(const c64* p) {
+  float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return c64(v.x, v.y);
+}
+template <> __device__ __forceinline__ c128 ldcg<c128>(const c128* p) {
+  double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return c128(v.x, v.y);
+}
+template <typename T> __device__ __forceinline__ void stcg(T* p, T v);
+template <> __device__ __forceinline__ void stcg<float>(float* p, float v) { __stcg(p, v); }
+template <> __device__ __forceinline__ void stcg<double>(double* p, double v) { __stcg(p, v); }
+template <> __device__ __forceinline__ void stcg<c64>(c64* p, c64 v) {
+  __stcg(reinterpret_cast<float2*>(p), make_float2(v.re, v.im));
+}
+template <> __device__ __forceinline__ void stcg<c128>(c128* p, c128 v) {
+  __stcg(reinterpret_cast<double2*>(p), make_double2(v.re, v.im));
+}
+
+// info[0] = first error recorded by the persistent launch (0 = none)
+static __global__ void copy_sync_error(const SyncWords* sw, int* info) {
+  int e = sw->err;
+  if (e) info[0] = e;
+}
+
+// Largest co-resident grid for a cooperative launch of `kernel`.
+inline int coop_capacity(const void* kernel, int threads, size_t smem) {
+  int dev = 0, sms = 0, per = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess) return 0;
+  return per * sms;
+}
+
+}  // namespace tnc

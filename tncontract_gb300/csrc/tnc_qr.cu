@@ -1,0 +1,231 @@
+// Reduced QR (np.linalg.qr(mode="reduced") in tensor_qr, tncontract/tensor.py:1044).
+//
+// Householder QR in LAPACK's convention (geqrf + ungqr: Q = H_0 ... H_{k-1},
+// H_c = I - tau_c v_c v_c^H, v_c[c] = 1, R's diagonal real for complex input),
+// run as ONE cooperative persistent launch organised as a column-owner
+// dataflow: every column of A is owned by one warp; reflector c is published
+// (with a flag) by the owner of column c as soon as reflectors 0..c-1 have
+// been applied to that column, and each warp applies the published
+// reflectors to its own columns in order.  The owner of column c+1 applies
+// reflector c to that column first and publishes reflector c+1 before
+// touching its other columns (look-ahead), which keeps the critical path at
+// one column update + one reflector per step.  No grid-wide barrier is needed.
+//
+// Working layout: Bt = A^T (row c of Bt is column c of A, contiguous), so
+// every warp streams its own column and the published reflector with
+// coalesced loads.  Q is formed by backward accumulation, each warp applying
+// H_{min(j,k-1)} ... H_0 to its own column e_j -- independent across warps.
+#include "tnc_persist.cuh"
+
+namespace tnc {
+
+constexpr int kQrWarps = 4;  // warps per CTA
+
+template <typename T>
+__device__ __forceinline__ T div_(T a, T b);
+template <> __device__ __forceinline__ float div_(float a, float b) { return a / b; }
+template <> __device__ __forceinline__ double div_(double a, double b) { return a / b; }
+template <typename R>
+__device__ __forceinline__ cplx<R> div_c(cplx<R> a, cplx<R> b) {
+  R d = b.re * b.re + b.im * b.im;
+  return cplx<R>((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
+}
+template <> __device__ __forceinline__ c64 div_(c64 a, c64 b) { return div_c(a, b); }
+template <> __device__ __forceinline__ c128 div_(c128 a, c128 b) { return div_c(a, b); }
+
+template <typename T> __device__ __forceinline__ typename traits<T>::real imag_(T v) {
+  if constexpr (traits<T>::is_complex) return v.im; else return 0;
+}
+
+// Reflector for column c (row c of Bt), LAPACK larfg convention.
+template <typename T>
+__device__ void make_reflector(T* col, int64_t c, int64_t m, T* tau_out) {
+  typedef typename traits<T>::real R;
+  const int lane = threadIdx.x & 31;
+  R xn = 0;
+  for (int64_t i = c + 1 + lane; i < m; i += 32) xn += abs2_(col[i]);
+  xn = warp_sum(xn);
+  T alpha = col[c];
+  T tau = zero_<T>();
+  if (!(xn == R(0) && imag_(alpha) == R(0))) {
+    R ar = real_(alpha);
+    R beta = -copysign(sqrt(abs2_(alpha) + xn), ar);
+    T betaT = from_real<T>(beta);
+    tau = div_(betaT - alpha, betaT);
+    T scal = div_(one_<T>(), alpha - betaT);
+    for (int64_t i = c + 1 + lane; i < m; i += 32) col[i] = scal * col[i];
+    __syncwarp();
+    if (lane == 0) col[c] = betaT;
+  }
+  if (lane == 0) *tau_out = tau;
+  __syncwarp();
+}
+
+// col[i] -= conj(tau) * (v^H col) * v[i], i >= c  (applies H_c^H)
+template <typename T>
+__device__ __forceinline__ void apply_reflector_h(T* col, const T* v, T tau, int64_t c, int64_t m) {
+  const int lane = threadIdx.x & 31;
+  T w = (lane == 0) ? col[c] : zero_<T>();
+  for (int64_t i = c + 1 + lane; i < m; i += 32) fma_(w, conj_(ldcg(v + i)), col[i]);
+  w = warp_sum(w);
+  T f = conj_(tau) * w;
+  if (lane == 0) col[c] = col[c] - f;
+  for (int64_t i = c + 1 + lane; i < m; i += 32) col[i] = col[i] - f * ldcg(v + i);
+  __syncwarp();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kQrWarps * 32)
+qr_factor_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) {
+  const int64_t k = m < n ? m : n;
+  const int64_t nwarps = (int64_t)gridDim.x * kQrWarps;
+  const int64_t wid = (int64_t)blockIdx.x * kQrWarps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (wid >= n) return;
+  // my columns: wid, wid + nwarps, ...
+  if (wid == 0) {  // column 0 needs no earlier reflector
+    make_reflector(Bt, 0, m, tau);
+    __threadfence();
+    if (lane == 0) atomicExch(&flags[0], 1);
+  }
+  int64_t first = wid;  // first own column not yet past all reflectors
+  for (int64_t c = 0; c < k; ++c) {
+    // skip own columns <= c: they are final (their reflector is published)
+    while (first <= c) first += nwarps;
+    if (first >= n) break;  // nothing left to update
+    if (!warp_wait_flag(&flags[c], sw)) return;
+    const T* v = Bt + c * m;
+    const T tc = ldcg(tau + c);
+    for (int64_t j = first; j < n; j += nwarps) {
+      apply_reflector_h(Bt + j * m, v, tc, c, m);
+      if (j == c + 1 && j < k) {  // look-ahead: publish the next reflector now
+        make_reflector(Bt + j * m, j, m, tau + j);
+        __threadfence();
+        if (lane == 0) atomicExch(&flags[j], 1);
+      }
+    }
+  }
+}
+
+// Qt[j] = H_{min(j,k-1)} ... H_0 e_j  (row j of Qt = column j of Q)
+template <typename T>
+__global__ void __launch_bounds__(kQrWarps * 32)
+qr_form_q_kernel(const T* __restrict__ Bt, int64_t m, int64_t k, const T* __restrict__ tau, T* __restrict__ Qt) {
+  const int64_t nwarps = (int64_t)gridDim.x * kQrWarps;
+  const int lane = threadIdx.x & 31;
+  for (int64_t j = (int64_t)blockIdx.x * kQrWarps + (threadIdx.x >> 5); j < k; j += nwarps) {
+    T* q = Qt + j * m;
+    for (int64_t i = lane; i < m; i += 32) q[i] = (i == j) ? one_<T>() : zero_<T>();
+    __syncwarp();
+    for (int64_t c = j; c >= 0; --c) {
+      const T* v = Bt + c * m;
+      const T tc = tau[c];
+      // q -= tau * (v^H q) * v  (H_c, not conjugated)
+      T w = (lane == 0) ? q[c] : zero_<T>();
+      for (int64_t i = c + 1 + lane; i < m; i += 32) fma_(w, conj_(v[i]), q[i]);
+      w = warp_sum(w);
+      T f = tc * w;
+      __syncwarp();
+      if (lane == 0) q[c] = q[c] - f;
+      for (int64_t i = c + 1 + lane; i < m; i += 32) q[i] = q[i] - f * v[i];
+      __syncwarp();
+    }
+  }
+}
+
+// R[i][j] = Bt[j][i] for i <= j, 0 below (R is k x n)
+template <typename T>
+__global__ void qr_extract_r(const T* __restrict__ Bt, int64_t m, int64_t n, int64_t k, T* __restrict__ R) {
+  const int64_t total = k * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / n, j = e - i * n;
+    R[e] = (i <= j) ? Bt[j * m + i] : zero_<T>();
+  }
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct QrLayout {
+  size_t bt, tau, flags, sync, qt, total;
+};
+static QrLayout qr_layout(int64_t m, int64_t n, size_t es) {
+  int64_t k = m < n ? m : n;
+  QrLayout L;
+  size_t off = 0;
+  L.bt = off; off = align256(off + (size_t)n * m * es);
+  L.tau = off; off = align256(off + (size_t)k * es);
+  L.flags = off; off = align256(off + (size_t)k * sizeof(int));
+  L.sync = off; off = align256(off + sizeof(SyncWords));
+  L.qt = off; off = align256(off + (size_t)k * m * es);
+  L.total = off;
+  return L;
+}
+
+template <typename T>
+static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, void* work, size_t wb,
+                   int* info, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || lda < n || !A || !Q || !R || !work || !info) return TNC_ERR_ARG;
+  QrLayout L = qr_layout(m, n, sizeof(T));
+  if (wb < L.total) return TNC_ERR_WORKSPACE;
+  const int64_t k = m < n ? m : n;
+  char* w = (char*)work;
+  T* Bt = (T*)(w + L.bt);
+  T* tau = (T*)(w + L.tau);
+  int* flags = (int*)(w + L.flags);
+  SyncWords* sw = (SyncWords*)(w + L.sync);
+  T* Qt = (T*)(w + L.qt);
+  // Bt = A^T (A may have lda > n: transpose through the GEMM-free permute
+  // path only handles dense input, so copy row blocks with a strided GEMM-less
+  // 2-D transpose)
+  if (lda == n) {
+    int64_t shp[2] = {m, n};
+    int perm[2] = {1, 0};
+    int s = tnc_permute(sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128),
+                        A, Bt, 2, shp, perm, 0, st);
+    if (s) return s;
+  } else {
+    return TNC_ERR_ARG;
+  }
+  if (cudaMemsetAsync(flags, 0, (size_t)k * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(info, 0, sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
+  const int threads = kQrWarps * 32;
+  int cap = coop_capacity((const void*)qr_factor_kernel<T>, threads, 0);
+  if (cap <= 0) return TNC_ERR_CUDA;
+  int64_t want = (n + kQrWarps - 1) / kQrWarps;
+  int grid = (int)(want < cap ? want : cap);
+  int64_t mm = m, nn = n;
+  void* args[] = {(void*)&Bt, (void*)&mm, (void*)&nn, (void*)&tau, (void*)&flags, (void*)&sw};
+  if (cudaLaunchCooperativeKernel((const void*)qr_factor_kernel<T>, dim3(grid), dim3(threads), args, 0, st) !=
+      cudaSuccess)
+    return TNC_ERR_CUDA;
+  copy_sync_error<<<1, 1, 0, st>>>(sw, info);
+  int64_t gq = (k + kQrWarps - 1) / kQrWarps;
+  if (gq > 152 * 16) gq = 152 * 16;
+  qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
+  qr_extract_r<T><<<grid1d(k * n, 256), 256, 0, st>>>(Bt, m, n, k, R);
+  if (launch_status()) return TNC_ERR_CUDA;
+  // Q = Qt^T
+  int64_t shp[2] = {k, m};
+  int perm[2] = {1, 0};
+  return tnc_permute(sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128),
+                     Qt, Q, 2, shp, perm, 0, st);
+}
+
+}  // namespace tnc
+
+using namespace tnc;
+
+extern "C" int tnc_qr_workspace_size(int dtype, int64_t m, int64_t n, size_t* bytes) {
+  int es = elem_size(dtype);
+  if (!es || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
+  *bytes = qr_layout(m, n, es).total;
+  return TNC_OK;
+}
+
+extern "C" int tnc_qr(int dtype, int64_t m, int64_t n, const void* A, int64_t lda, void* Q, void* R, void* work,
+                      size_t work_bytes, int* info, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  TNC_DISPATCH(dtype, T, return qr_impl<T>(m, n, (const T*)A, lda, (T*)Q, (T*)R, work, work_bytes, info, st));
+  return TNC_ERR_ARG;
+}

@@ -1,0 +1,280 @@
+// Thin SVD (np.linalg.svd(full_matrices=False) in tensor_svd,
+// tncontract/tensor.py:915, and its scipy gesvd retry, :916-929).
+//
+// One-sided (Hestenes) Jacobi on the ROWS of a working matrix W (nr x L,
+// nr <= L): pairs of rows are rotated until all rows are mutually orthogonal
+// to within tol.  The rotations are accumulated into J (nr x nr, rows), so
+//   W0 = J^H W,  W = D Y  (D = row norms, Y orthonormal rows)
+// is an SVD of the original W0 = (J^H) D Y.  For a wide A (m <= n) W0 = A;
+// for a tall A, W0 = A^H and the roles of U and V swap.
+//
+// Parallel ordering: round-robin tournament over the rows (nr-1 rounds of
+// nr/2 disjoint pairs per sweep), one warp per pair, the whole iteration in
+// ONE cooperative persistent launch with a bounded grid barrier between
+// rounds.  A sweep with no rotation ends the iteration (convergence); the
+// number of sweeps is capped and reported.  Finally the rows are sorted by
+// norm (descending, stable) and U, S, VH are written.
+//
+// Rotation for rows x (=w_p), y (=w_q): a=|x|^2, b=|y|^2, g=<x,y>=sum x conj(y),
+// h=|g|, e=g/h, tau=(b-a)/(2h), t=sign(tau)/(|tau|+sqrt(1+tau^2)),
+// c=1/sqrt(1+t^2), s=c t:   x' = c x - s e y,   y' = s conj(e) x + c y.
+// This is the 2x2 Hermitian Jacobi rotation of the Gram matrix [[a,g],[g*,b]]
+// (Golub & Van Loan, sec. 8.5 and 8.6.3), applied to rows.
+#include "tnc_persist.cuh"
+
+namespace tnc {
+
+constexpr int kSvdWarps = 2;  // warps per CTA (spreads the pairs over many SMs)
+
+template <typename T>
+__device__ __forceinline__ void pair_indices(int64_t np, int64_t r, int64_t i, int64_t& p, int64_t& q) {
+  const int64_t mod = np - 1;
+  if (i == 0) { p = r; q = mod; }
+  else { p = (r + i) % mod; q = (r - i + mod) % mod; }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSvdWarps * 32)
+jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, unsigned* counters, SyncWords* sw,
+              int* info) {
+  typedef typename traits<T>::real R;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * kSvdWarps + (threadIdx.x >> 5);
+  const int64_t nwarps = (int64_t)gridDim.x * kSvdWarps;
+  const int64_t np = nr + (nr & 1);
+  const int64_t npairs = np / 2;
+  const R rtol = (R)tol;
+  int sweep = 0;
+  bool converged = false;
+  unsigned last_rot = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    unsigned rot = 0;
+    for (int64_t r = 0; r < np - 1; ++r) {
+      for (int64_t pi = gw; pi < npairs; pi += nwarps) {
+        int64_t p, q;
+        pair_indices<T>(np, r, pi, p, q);
+        if (p >= nr || q >= nr) continue;
+        T* x = W + p * L;
+        T* y = W + q * L;
+        R a = 0, b = 0;
+        T g = zero_<T>();
+        for (int64_t k = lane; k < L; k += 32) {
+          T xv = ldcg(x + k), yv = ldcg(y + k);
+          a += abs2_(xv);
+          b += abs2_(yv);
+          fma_(g, xv, conj_(yv));
+        }
+        a = warp_sum(a);
+        b = warp_sum(b);
+        g = warp_sum(g);
+        const R h = sqrt(abs2_(g));
+        if (!(h > rtol * sqrt(a) * sqrt(b))) continue;  // also skips NaN / zero rows
+        const R tau = (b - a) / (2 * h);
+        R t;
+        if (fabs(tau) > (R)1e15) t = (R)0.5 / tau;
+        else t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
+        const R c = R(1) / sqrt(R(1) + t * t);
+        const R s = c * t;
+        const T e = g * (R(1) / h);
+        const T se = s * e, sec = s * conj_(e);
+        for (int64_t k = lane; k < L; k += 32) {
+          T xv = ldcg(x + k), yv = ldcg(y + k);
+          stcg(x + k, c * xv - se * yv);
+          stcg(y + k, sec * xv + c * yv);
+        }
+        T* xj = J + p * nr;
+        T* yj = J + q * nr;
+        for (int64_t k = lane; k < nr; k += 32) {
+          T xv = ldcg(xj + k), yv = ldcg(yj + k);
+          stcg(xj + k, c * xv - se * yv);
+          stcg(yj + k, sec * xv + c * yv);
+        }
+        ++rot;
+      }
+      if (!grid_barrier(sw, gridDim.x)) return;
+    }
+    if (lane == 0 && rot) atomicAdd(&counters[sweep], rot);
+    if (!grid_barrier(sw, gridDim.x)) return;
+    last_rot = ld_volatile(&counters[sweep]);
+    if (last_rot == 0) { converged = true; ++sweep; break; }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    info[0] = converged ? TNC_OK : TNC_ERR_NOT_CONVERGED;
+    info[1] = sweep;
+    info[2] = (int)last_rot;
+  }
+}
+
+// J = identity, W <- W0 (already in place)
+template <typename T>
+__global__ void eye_kernel(T* J, int64_t n) {
+  const int64_t total = n * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / n, j = e - i * n;
+    J[e] = (i == j) ? one_<T>() : zero_<T>();
+  }
+}
+
+template <typename T>
+__global__ void row_norms_kernel(const T* W, int64_t nr, int64_t L, typename traits<T>::real* D, int* info) {
+  typedef typename traits<T>::real R;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < nr; i += nw) {
+    double acc = 0.0;
+    for (int64_t k = lane; k < L; k += 32) acc += (double)abs2_(W[i * L + k]);
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      D[i] = (R)sqrt(acc);
+      if (!isfinite(acc)) atomicExch(info, TNC_ERR_NONFINITE);
+    }
+  }
+}
+
+// pos[i] = #{j: D_j > D_i} + #{j < i: D_j == D_i}  (stable descending order)
+template <typename R>
+__global__ void rank_kernel(const R* D, int64_t n, int64_t* pos) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    R di = D[i];
+    int64_t c = 0;
+    for (int64_t j = 0; j < n; ++j) {
+      R dj = D[j];
+      c += (dj > di) || (dj == di && j < i);
+    }
+    pos[i] = c;
+  }
+}
+
+// wide (W0 = A, nr = m, L = n):  U[r][pos_i] = conj(J[i][r]); VH[pos_i][:] = W[i][:]/D_i
+// tall (W0 = A^H, nr = n, L = m): U[r][pos_i] = conj(W[i][r])/D_i; VH[pos_i][:] = J[i][:]
+template <typename T>
+__global__ void svd_output_kernel(const T* W, const T* J, const typename traits<T>::real* D, const int64_t* pos,
+                                  int64_t nr, int64_t L, int tall, T* U, typename traits<T>::real* S, T* VH) {
+  typedef typename traits<T>::real R;
+  // part 1: rows of length L of W -> (wide) VH rows / (tall) U columns
+  const int64_t t1 = nr * L;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < t1; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / L, r = e - i * L;
+    R d = D[i];
+    T v = W[e];
+    T o = (d > R(0)) ? v * (R(1) / d) : zero_<T>();
+    if (tall) U[r * nr + pos[i]] = conj_(o);
+    else VH[pos[i] * L + r] = o;
+    if (r == 0) S[pos[i]] = d;
+  }
+  // part 2: rows of J -> (wide) U columns / (tall) VH rows
+  const int64_t t2 = nr * nr;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < t2; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e / nr, r = e - i * nr;
+    T v = J[e];
+    if (tall) VH[pos[i] * nr + r] = v;
+    else U[r * nr + pos[i]] = conj_(v);
+  }
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct SvdLayout {
+  size_t w, j, d, pos, counters, sync, total;
+};
+static const int kMaxSweepsCap = 100;
+static SvdLayout svd_layout(int64_t m, int64_t n, size_t es, size_t rs) {
+  int64_t nr = m < n ? m : n, L = m < n ? n : m;
+  SvdLayout Ly;
+  size_t off = 0;
+  Ly.w = off; off = align256(off + (size_t)nr * L * es);
+  Ly.j = off; off = align256(off + (size_t)nr * nr * es);
+  Ly.d = off; off = align256(off + (size_t)nr * rs);
+  Ly.pos = off; off = align256(off + (size_t)nr * sizeof(int64_t));
+  Ly.counters = off; off = align256(off + kMaxSweepsCap * sizeof(unsigned));
+  Ly.sync = off; off = align256(off + sizeof(SyncWords));
+  Ly.total = off;
+  return Ly;
+}
+
+template <typename T> static int dtype_of();
+template <> int dtype_of<float>() { return TNC_F32; }
+template <> int dtype_of<double>() { return TNC_F64; }
+template <> int dtype_of<c64>() { return TNC_C64; }
+template <> int dtype_of<c128>() { return TNC_C128; }
+
+template <typename T>
+static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typename traits<T>::real* S, T* VH,
+                    int max_sweeps, double tol, void* work, size_t wb, int* info, cudaStream_t st) {
+  typedef typename traits<T>::real R;
+  if (m <= 0 || n <= 0 || lda != n || !A || !U || !S || !VH || !work || !info) return TNC_ERR_ARG;
+  SvdLayout Ly = svd_layout(m, n, sizeof(T), sizeof(R));
+  if (wb < Ly.total) return TNC_ERR_WORKSPACE;
+  if (max_sweeps <= 0) max_sweeps = 40;
+  if (max_sweeps > kMaxSweepsCap) max_sweeps = kMaxSweepsCap;
+  const int tall = m > n;
+  const int64_t nr = tall ? n : m, L = tall ? m : n;
+  if (tol <= 0) {
+    double sl = sqrt((double)(L > 8 ? L : 8));
+    tol = sl * traits<T>::eps * (sizeof(R) == 4 ? 4.0 : 1.0);
+  }
+  char* w = (char*)work;
+  T* W = (T*)(w + Ly.w);
+  T* J = (T*)(w + Ly.j);
+  R* D = (R*)(w + Ly.d);
+  int64_t* pos = (int64_t*)(w + Ly.pos);
+  unsigned* counters = (unsigned*)(w + Ly.counters);
+  SyncWords* sw = (SyncWords*)(w + Ly.sync);
+  int s;
+  if (tall) {  // W = A^H (n x m)
+    int64_t shp[2] = {m, n};
+    int perm[2] = {1, 0};
+    s = tnc_permute(dtype_of<T>(), A, W, 2, shp, perm, 1, st);
+  } else {
+    s = cudaMemcpyAsync(W, A, (size_t)m * n * sizeof(T), cudaMemcpyDeviceToDevice, st) == cudaSuccess ? TNC_OK
+                                                                                                       : TNC_ERR_CUDA;
+  }
+  if (s) return s;
+  eye_kernel<T><<<grid1d(nr * nr, 256), 256, 0, st>>>(J, nr);
+  if (cudaMemsetAsync(counters, 0, kMaxSweepsCap * sizeof(unsigned), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(info, 0, 4 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (launch_status()) return TNC_ERR_CUDA;
+  if (nr > 1) {
+    const int threads = kSvdWarps * 32;
+    int cap = coop_capacity((const void*)jacobi_kernel<T>, threads, 0);
+    if (cap <= 0) return TNC_ERR_CUDA;
+    int64_t npairs = (nr + 1) / 2;
+    int64_t want = (npairs + kSvdWarps - 1) / kSvdWarps;
+    int grid = (int)(want < cap ? want : cap);
+    int64_t nr_ = nr, L_ = L;
+    int ms = max_sweeps;
+    double tl = tol;
+    void* args[] = {(void*)&W, (void*)&J, (void*)&nr_, (void*)&L_, (void*)&ms, (void*)&tl,
+                    (void*)&counters, (void*)&sw, (void*)&info};
+    if (cudaLaunchCooperativeKernel((const void*)jacobi_kernel<T>, dim3(grid), dim3(threads), args, 0, st) !=
+        cudaSuccess)
+      return TNC_ERR_CUDA;
+  }
+  copy_sync_error<<<1, 1, 0, st>>>(sw, info);
+  row_norms_kernel<T><<<grid1d(nr * 32, 256), 256, 0, st>>>(W, nr, L, D, info);
+  rank_kernel<R><<<grid1d(nr, 128), 128, 0, st>>>(D, nr, pos);
+  svd_output_kernel<T><<<grid1d(nr * L, 256), 256, 0, st>>>(W, J, D, pos, nr, L, tall, U, S, VH);
+  return launch_status();
+}
+
+}  // namespace tnc
+
+using namespace tnc;
+
+extern "C" int tnc_svd_workspace_size(int dtype, int64_t m, int64_t n, size_t* bytes) {
+  int es = elem_size(dtype);
+  if (!es || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
+  size_t rs = (dtype == TNC_F32 || dtype == TNC_C64) ? 4 : 8;
+  *bytes = svd_layout(m, n, es, rs).total;
+  return TNC_OK;
+}
+
+extern "C" int tnc_svd(int dtype, int64_t m, int64_t n, const void* A, int64_t lda, void* U, void* S, void* VH,
+                       int max_sweeps, double tol, void* work, size_t work_bytes, int* info, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  TNC_DISPATCH(dtype, T,
+               return svd_impl<T>(m, n, (const T*)A, lda, (T*)U, (typename traits<T>::real*)S, (T*)VH, max_sweeps,
+                                  tol, work, work_bytes, info, st));
+  return TNC_ERR_ARG;
+}

@@ -1,0 +1,656 @@
+"""Labelled tensors on the GPU: the drop-in for tncontract/tensor.py.
+
+``Tensor.data`` is a dense, C-contiguous CUDA ``torch.Tensor``; ``labels`` is
+a host list of strings.  Label -> axis resolution and every label-order rule
+are restated exactly from the reference (each method cites its
+``tensor.py`` lines); the data work (axis permutations, tensordot, SVD, QR,
+norms, traces, scaling) runs in the native sm_103a library through
+``tncontract_gb300._ops``.  Sequences of axis moves the reference performs
+one ``np.rollaxis`` at a time are first simulated on the host and then
+applied as ONE device permutation.
+
+Differences a user can see: ``data`` is a CUDA tensor (``to_numpy()`` gives
+a host copy); scalar results of norms are Python floats; ``truncated_svd``
+returns the discarded singular values as a device tensor.
+"""
+from __future__ import annotations
+
+import copy as _copy
+
+import numpy as np
+import torch
+
+from . import _ops
+from . import label as lbl
+
+__all__ = ['Tensor', 'contract', 'distance', 'matrix_to_tensor',
+           'tensor_to_matrix', 'random_tensor', 'tensor_product', 'tensor_svd',
+           'truncated_svd', 'zeros_tensor']
+
+
+# --------------------------------------------------------------------------
+# host-side simulation of axis moves
+# --------------------------------------------------------------------------
+
+
+class _Axes:
+    """Tracks (label, original axis) pairs through move_index / rollaxis so a
+    chain of moves becomes one permutation."""
+
+    def __init__(self, labels):
+        self.items = [(l, i) for i, l in enumerate(labels)]
+
+    @property
+    def labels(self):
+        return [l for l, _ in self.items]
+
+    @property
+    def perm(self):
+        return [i for _, i in self.items]
+
+    def rollaxis(self, axis, start):
+        item = self.items.pop(axis)
+        if start > axis:
+            start -= 1
+        self.items.insert(start, item)
+
+    def move_index(self, label, position):
+        # tensor.py:380-394 (first index carrying `label`)
+        index = self.labels.index(label)
+        item = self.items.pop(index)
+        self.items.insert(position, item)
+
+
+def _new(data, labels):
+    """Wrap an owned device tensor without copying."""
+    t = Tensor.__new__(Tensor)
+    t.data = data
+    t.labels = labels
+    return t
+
+
+class Tensor():
+    """A device array plus a list of labels, one per axis (``tensor.py:16-56``).
+
+    The constructor copies ``data`` to the current CUDA device (the reference
+    copies with ``np.array``, ``:48``); integer input becomes float64."""
+
+    def __init__(self, data, labels=None, base_label="i"):
+        labels = [] if labels is None else labels
+        self.data = _ops.to_device(data)
+        if len(labels) == 0:
+            self.assign_labels(base_label=base_label)
+        else:
+            self.labels = labels
+
+    # ---------------------------------------------------------------- display
+    def __repr__(self):
+        return "Tensor(data=%r, labels=%r)" % (self.data, self.labels)
+
+    def __str__(self):
+        lines = []
+        for i, label in enumerate(self.labels):
+            lines.append("   " + str(i) + ". (dim=" + str(self.shape[i]) + ") " + str(label) + "\n")
+        return ("Tensor object: \n" + "Data type: " + str(self.data.dtype) + "\n"
+                "Number of indices: " + str(self.data.dim()) + "\n"
+                "\nIndex labels:\n" + "".join(lines))
+
+    def to_numpy(self):
+        """Host copy of ``data`` as a NumPy array."""
+        return self.data.detach().cpu().numpy()
+
+    # ---------------------------------------------------------------- algebra
+    def __eq__(self, other):
+        if isinstance(other, Tensor):
+            return (tuple(self.data.shape) == tuple(other.data.shape)
+                    and self.data.dtype == other.data.dtype
+                    and bool(torch.equal(self.data, other.data))
+                    and self.labels == other.labels)
+        return False
+
+    def __neq__(self, other):
+        return not self.__eq__(other)
+
+    def _scaled(self, other):
+        try:
+            z = complex(other)
+        except TypeError:
+            raise TypeError("unsupported operand type(s) *: for '" + self.__class__.__name__
+                            + "' and '" + other.__class__.__name__ + "'")
+        data = self.data
+        if z.imag != 0 and not _ops.is_complex(data.dtype):
+            data = _ops.cast(data, torch.complex128 if data.dtype == torch.float64 else torch.complex64)
+        return _new(_ops.scale(data, z), list(self.labels))
+
+    def __mul__(self, other):
+        """``tensor.py:95-108``: a copy scaled by a number."""
+        return self._scaled(other)
+
+    def __rmul__(self, other):
+        """``tensor.py:110-123``"""
+        return self._scaled(other)
+
+    def __add__(self, other):
+        """``tensor.py:125-140``: consolidated copies added elementwise."""
+        try:
+            a = self.copy()
+            b = other.copy()
+            a.consolidate_indices()
+            b.consolidate_indices()
+            if a.labels != b.labels or tuple(a.shape) != tuple(b.shape):
+                raise ValueError
+            dt = torch.promote_types(a.data.dtype, b.data.dtype)
+            out = _ops.cast(b.data, dt).clone()
+            _ops.axpby(1.0, _ops.cast(a.data, dt), 1.0, out)
+            return _new(out, a.labels)
+        except Exception:
+            raise TypeError("Can only add together tensors with the same" +
+                            " indices: labels and dimensions of each index must match.")
+
+    def __getitem__(self, *args):
+        """``tensor.py:142-145``: ``A["a", "b"] * B["c", "d"]`` shorthand."""
+        return ToContract(self, *args)
+
+    # ---------------------------------------------------------------- labels
+    def get_labels(self):
+        return self._labels
+
+    def set_labels(self, labels):
+        # tensor.py:151-155
+        if len(labels) == self.data.dim():
+            self._labels = list(labels)
+        else:
+            raise ValueError("Labels do not match shape of data.")
+
+    labels = property(get_labels, set_labels)
+
+    def assign_labels(self, base_label="i"):
+        """``tensor.py:159-162``"""
+        self.labels = [base_label + str(i) for i in range(self.data.dim())]
+
+    def replace_label(self, old_labels, new_labels):
+        """``tensor.py:164-181``"""
+        if not isinstance(old_labels, list):
+            old_labels = [old_labels]
+        if not isinstance(new_labels, list):
+            new_labels = [new_labels]
+        for i, label in enumerate(self.labels):
+            if label in old_labels:
+                self.labels[i] = new_labels[old_labels.index(label)]
+
+    def prime_label(self, labels=None):
+        """``tensor.py:183-201``"""
+        if labels is None:
+            labels = self.labels
+        elif not isinstance(labels, list):
+            labels = [labels]
+        for i, label in enumerate(self.labels):
+            for noprime in labels:
+                if lbl.noprime_label(label) == noprime:
+                    self.labels[i] = lbl.prime_label(self.labels[i])
+
+    def unprime_label(self, labels=None):
+        """``tensor.py:203-236``"""
+        if labels is None:
+            labels = self.labels
+        elif not isinstance(labels, list):
+            labels = [labels]
+        for i, label in enumerate(self.labels):
+            for noprime in labels:
+                if lbl.noprime_label(label) == noprime:
+                    self.labels[i] = lbl.unprime_label(self.labels[i])
+
+    def add_suffix_to_labels(self, suffix):
+        """``tensor.py:490-497``"""
+        self.labels = [label + suffix for label in self.labels]
+
+    def suf(self, suffix):
+        """``tensor.py:499-504``: copy with ``suffix`` on every label."""
+        t = self.copy()
+        t.labels = [x + suffix for x in t.labels]
+        return t
+
+    # ---------------------------------------------------------------- axes
+    def _apply(self, axes, shape=None):
+        """Materialise a simulated chain of moves as one device permute."""
+        self.data = _ops.permute(self.data, axes.perm)
+        if shape is not None:
+            self.data = self.data.reshape(tuple(shape))
+
+    def move_index(self, label, position):
+        """``tensor.py:380-394``"""
+        ax = _Axes(self.labels)
+        ax.move_index(label, position)
+        self._apply(ax)
+        self._labels = ax.labels
+
+    def move_indices(self, labels, position, preserve_relative_order=False):
+        """``tensor.py:396-482``"""
+        if not isinstance(labels, list):
+            labels = [labels]
+        ax = _Axes(self.labels)
+        n_move = 0
+        if preserve_relative_order:
+            for label in list(self.labels):
+                if label in labels:
+                    ax.move_index(label, len(ax.items) - 1)
+                    n_move += 1
+        else:
+            unique = []
+            for label in labels:
+                if label not in unique:
+                    unique.append(label)
+            for label in unique:
+                for _ in range(ax.labels.count(label)):
+                    ax.move_index(label, len(ax.items) - 1)
+                    n_move += 1
+        if position + n_move > len(ax.items):
+            raise ValueError("Specified position too far right.")
+        for j in range(n_move):
+            old = len(ax.items) - n_move + j
+            ax.rollaxis(old, position + j)
+        self._apply(ax)
+        self._labels = ax.labels
+
+    def consolidate_indices(self, labels=[]):
+        """``tensor.py:340-370``: fuse axes sharing a label (first occurrence
+        most significant); labels visited in sorted order."""
+        uniq = sorted(set(self.labels))
+        if len(labels) != 0:
+            uniq = [x for x in uniq if x in labels]
+        groups = [(l, [i]) for i, l in enumerate(self.labels)]  # (label, axes)
+        for p, label in enumerate(uniq):
+            # positions are taken before the rolls; every occurrence lies at or
+            # after p + k, so np.rollaxis(q -> p + k) is a pop/insert
+            idx = [i for i, g in enumerate(groups) if g[0] == label]
+            for k, q in enumerate(idx):
+                groups.insert(p + k, groups.pop(q))
+            n = len(idx)
+            fused = (label, [a for g in groups[p:p + n] for a in g[1]])
+            groups[p:p + n] = [fused]
+        perm = [a for g in groups for a in g[1]]
+        shape = [int(np.prod([self.data.shape[a] for a in g[1]], dtype=np.int64)) for g in groups]
+        self.data = _ops.permute(self.data, perm).reshape(tuple(shape))
+        self._labels = [g[0] for g in groups]
+
+    def sort_labels(self):
+        self.consolidate_indices()
+
+    def fuse_indices(self, indices_to_fuse, new_label, preserve_relative_order=False):
+        """``tensor.py:238-297``"""
+        self.move_indices(indices_to_fuse, 0, preserve_relative_order=preserve_relative_order)
+        total_dim = 1
+        last_idx = None
+        for i, x in enumerate(self.labels):
+            if x in indices_to_fuse:
+                total_dim *= self.data.shape[i]
+                last_idx = i
+        new_labels = [new_label] + self.labels[last_idx + 1:]
+        new_shape = (total_dim,) + tuple(self.data.shape[last_idx + 1:])
+        self.data = self.data.reshape(new_shape)
+        self.labels = new_labels
+
+    def split_index(self, label, new_dims, new_labels):
+        """``tensor.py:299-316``"""
+        if len(new_dims) != len(new_labels):
+            raise ValueError("Length of new_dims must equal length of new_labels")
+        i = self.labels.index(label)
+        new_shape = tuple(self.data.shape[:i]) + tuple(new_dims) + tuple(self.data.shape[i + 1:])
+        new_labels = self.labels[:i] + list(new_labels) + self.labels[i + 1:]
+        self.data = self.data.reshape(new_shape)
+        self.labels = new_labels
+
+    def contract_internal(self, label1, label2, index1=0, index2=0):
+        """``tensor.py:318-334``: trace over two labelled axes."""
+        i1 = [i for i, x in enumerate(self.labels) if x == label1][index1]
+        i2 = [i for i, x in enumerate(self.labels) if x == label2][index2]
+        if self.data.shape[i1] != self.data.shape[i2]:
+            raise ValueError("diag requires an array of at least two dimensions "
+                             "with equal axis lengths")
+        self.data = _ops.trace(self.data, i1, i2)
+        self.labels = [l for j, l in enumerate(self.labels) if j not in (i1, i2)]
+
+    trace = contract_internal
+    tr = contract_internal
+
+    def add_dummy_index(self, label, position=0):
+        """``tensor.py:506-513``"""
+        self.data = self.data.unsqueeze(0)
+        self.labels.insert(0, label)
+        self.move_index(label, position)
+
+    def remove_all_dummy_indices(self, labels=None):
+        """``tensor.py:515-529`` (same iteration over the original label list)."""
+        orig_shape = tuple(self.shape)
+        for i, x in enumerate(self.labels):
+            if labels is not None:
+                if x in labels and orig_shape[i] == 1:
+                    self.move_index(x, 0)
+                    self.data = self.data[0]
+                    self.labels = self.labels[1:]
+            elif orig_shape[i] == 1:
+                self.move_index(x, 0)
+                self.data = self.data[0]
+                self.labels = self.labels[1:]
+
+    def index_dimension(self, label):
+        """``tensor.py:531-534``"""
+        return self.data.shape[self.labels.index(label)]
+
+    def to_matrix(self, row_labels):
+        return tensor_to_matrix(self, row_labels)
+
+    def pad_index(self, label, inc, before=False):
+        """``tensor.py:543-563``: zero padding of one axis."""
+        index = self.labels.index(label)
+        old = tuple(self.data.shape)
+        shp = list(old)
+        shp[index] += inc
+        out = _ops.zeros(shp, self.data.dtype)
+        outer = int(np.prod(old[:index], dtype=np.int64))
+        inner = int(np.prod(old[index + 1:], dtype=np.int64))
+        # rows = outer blocks; each block is (dim * inner) contiguous elements
+        _ops.copy2d(self.data.contiguous(), outer, old[index] * inner, old[index] * inner,
+                    out, shp[index] * inner, dst_off=(inc * inner if before else 0))
+        self.data = out
+
+    def conjugate(self):
+        """``tensor.py:484-485``"""
+        self.data = _ops.conj(self.data)
+
+    def inv(self):
+        """``tensor.py:487-488`` (matrix inverse; off the hot path, computed by
+        the library QR: inv(A) = R^-1 Q^H with a triangular solve in torch)."""
+        Q, R = _ops.qr(self.data)
+        eye = torch.eye(R.shape[0], dtype=R.dtype, device=R.device)
+        rinv = torch.linalg.solve_triangular(R, eye, upper=True)
+        self.data = _ops.matmul(rinv, Q, opB=2)
+
+    def copy(self):
+        """``tensor.py:372-378``"""
+        return _new(self.data.clone(), _copy.copy(self.labels))
+
+    def contract(self, *args, **kwargs):
+        """``tensor.py:565-577``: in-place form of :func:`contract`."""
+        t = contract(self, *args, **kwargs)
+        self.data = t.data
+        self.labels = t.labels
+
+    @property
+    def shape(self):
+        return tuple(self.data.shape)
+
+    @property
+    def rank(self):
+        return len(self.shape)
+
+    def norm(self):
+        """``tensor.py:587-590``: Frobenius norm (Python float)."""
+        return _ops.nrm2(self.data)
+
+
+class ToContract():
+    """``tensor.py:593-613``"""
+
+    def __init__(self, tensor, labels):
+        self.tensor = tensor
+        self.labels = labels
+
+    def __mul__(self, other):
+        labels1 = list(self.labels) if isinstance(self.labels, tuple) else self.labels
+        labels2 = list(other.labels) if isinstance(other.labels, tuple) else other.labels
+        return contract(self.tensor, other.tensor, labels1, labels2)
+
+
+# --------------------------------------------------------------------------
+# constructors
+# --------------------------------------------------------------------------
+
+
+def random_tensor(*args, **kwargs):
+    """``tensor.py:618-623`` (entries uniform in [0, 1) from NumPy's global RNG)."""
+    labels = kwargs.pop("labels", [])
+    base_label = kwargs.pop("base_label", "i")
+    return Tensor(np.random.rand(*args), labels=labels, base_label=base_label)
+
+
+def zeros_tensor(*args, **kwargs):
+    """``tensor.py:626-632``"""
+    labels = kwargs.pop("labels", [])
+    dtype = kwargs.pop("dtype", float)
+    base_label = kwargs.pop("base_label", "i")
+    return Tensor(np.zeros(*args, dtype=dtype), labels=labels, base_label=base_label)
+
+
+# --------------------------------------------------------------------------
+# contraction
+# --------------------------------------------------------------------------
+
+
+def _resolve(tensor1, tensor2, labels1, labels2, index_slice1, index_slice2):
+    """Label -> axis resolution of ``contract``, ``tensor.py:702-731``."""
+    if not isinstance(labels1, list):
+        labels1 = [labels1]
+    if not isinstance(labels2, list):
+        labels2 = [labels2]
+    ax1 = []
+    for label in labels1:
+        ax1.extend([i for i, x in enumerate(tensor1.labels) if x == label])
+    ax2 = []
+    for label in labels2:
+        ax2.extend([i for i, x in enumerate(tensor2.labels) if x == label])
+    if index_slice1 is not None:
+        index_slice1 = [x if x != -1 else len(ax1) - 1 for x in index_slice1]
+        ax1 = [j for i, j in enumerate(ax1) if i in index_slice1]
+    if index_slice2 is not None:
+        index_slice2 = [x if x != -1 else len(ax2) - 1 for x in index_slice2]
+        ax2 = [j for i, j in enumerate(ax2) if i in index_slice2]
+    return labels1, labels2, ax1, ax2
+
+
+def contract(tensor1, tensor2, labels1, labels2, index_slice1=None, index_slice2=None):
+    """Contract the axes of ``tensor1`` labelled ``labels1`` with those of
+    ``tensor2`` labelled ``labels2`` (``tensor.py:635-770``).
+
+    Every axis carrying a listed label takes part (repeated labels included);
+    ``index_slice`` selects a subset (``-1`` = last).  The result's labels are
+    the uncontracted labels of ``tensor1`` then ``tensor2`` in their original
+    order.  Mismatches raise the reference's ``ValueError`` diagnostics."""
+    labels1, labels2, ax1, ax2 = _resolve(tensor1, tensor2, labels1, labels2,
+                                          index_slice1, index_slice2)
+    ok = len(ax1) == len(ax2) and all(
+        tensor1.data.shape[a] == tensor2.data.shape[b] for a, b in zip(ax1, ax2))
+    if not ok:
+        # diagnostics in the reference's order, tensor.py:737-760
+        if not len(ax1) == len(ax2):
+            raise ValueError('Number of indices in contraction does not match.')
+        for i in range(len(ax1)):
+            d1 = tensor1.data.shape[ax1[i]]
+            d2 = tensor2.data.shape[ax2[i]]
+            if d1 != d2:
+                raise ValueError(labels1[i] + ' with dim=' + str(d1) + ' does not match '
+                                 + labels2[i] + ' with dim=' + str(d2))
+        for i in range(len(labels1)):
+            if not labels1[i] in tensor1.labels:
+                raise ValueError(labels1[i] + ' not in list of labels for tensor1')
+            if not labels2[i] in tensor2.labels:
+                raise ValueError(labels2[i] + ' not in list of labels for tensor2')
+        raise ValueError("shape-mismatch for sum")
+    data = _ops.tensordot(tensor1.data, tensor2.data, ax1, ax2)
+    new1 = [l for j, l in enumerate(tensor1.labels) if j not in ax1]
+    new2 = [l for j, l in enumerate(tensor2.labels) if j not in ax2]
+    return _new(data, new1 + new2)
+
+
+def tensor_product(*args):
+    """``tensor.py:773-779``"""
+    t = args[0]
+    for x in args[1:]:
+        t = contract(t, x, [], [])
+    return t
+
+
+def distance(tensor1, tensor2):
+    """``tensor.py:782-802``: Frobenius distance of consolidated copies."""
+    t1 = tensor1.copy()
+    t2 = tensor2.copy()
+    t1.consolidate_indices()
+    t2.consolidate_indices()
+    if t1.labels == t2.labels:
+        dt = torch.promote_types(t1.data.dtype, t2.data.dtype)
+        diff = _ops.cast(t1.data, dt).clone()
+        _ops.axpby(-1.0, _ops.cast(t2.data, dt), 1.0, diff)
+        return _ops.nrm2(diff)
+    raise ValueError("Input tensors must have the same labels.")
+
+
+def tensor_to_matrix(tensor, row_labels):
+    """``tensor.py:805-818``"""
+    ax = _Axes(tensor.labels)
+    for i, label in enumerate(row_labels):
+        ax.move_index(label, i)
+    data = _ops.permute(tensor.data, ax.perm)
+    nrow = int(np.prod(data.shape[:len(row_labels)], dtype=np.int64))
+    ncol = data.numel() // nrow if nrow else 0
+    return data.reshape(nrow, ncol)
+
+
+def matrix_to_tensor(matrix, shape, labels=None):
+    """``tensor.py:821-827``"""
+    labels = [] if labels is None else labels
+    if isinstance(matrix, torch.Tensor):
+        return Tensor(matrix.reshape(tuple(shape)), labels)
+    return Tensor(np.reshape(np.array(matrix), shape), labels)
+
+
+# --------------------------------------------------------------------------
+# factorisations
+# --------------------------------------------------------------------------
+
+
+def _matricise(tensor, row_labels):
+    """Row labels moved to the front one ``move_index`` at a time
+    (``tensor.py:903-912``), then one device permute and a reshape."""
+    ax = _Axes(tensor.labels)
+    for i, label in enumerate(row_labels):
+        ax.move_index(label, i)
+    data = _ops.permute(tensor.data, ax.perm)
+    shape = tuple(data.shape)
+    nrow = int(np.prod(shape[:len(row_labels)], dtype=np.int64))
+    ncol = int(np.prod(shape[len(row_labels):], dtype=np.int64))
+    return data.reshape(nrow, ncol), shape, ax.labels
+
+
+def _svd_parts(tensor, row_labels, svd_label):
+    mat, old_shape, labels = _matricise(tensor, row_labels)
+    column_labels = [x for x in labels if x not in row_labels]
+    u, s, v = _ops.svd(mat)
+    U = _new(u.reshape(tuple(old_shape[:len(row_labels)]) + (u.shape[1],)),
+             list(row_labels) + [svd_label + "in"])
+    V = _new(v.reshape((v.shape[0],) + tuple(old_shape[len(row_labels):])),
+             [svd_label + "out"] + column_labels)
+    return U, s, V
+
+
+def _S_tensor(s, dtype, svd_label):
+    S = _new(_ops.diag_matrix(s, dtype), [svd_label + "out", svd_label + "in"])
+    S._diag = s
+    return S
+
+
+def _absorb(U, s, V, how, svd_label):
+    """Absorb S into U ("left"), V ("right") or sqrt(S) into both; the same
+    result as the reference's contractions with the dense diag(S)
+    (``tensor.py:944-959, 1166-1182``) computed as a row/column scaling.
+    The reference contracts over the literal labels "svd_in"/"svd_out"; with
+    another ``svd_label`` that is an outer product, reproduced by contract."""
+    if svd_label != "svd_":
+        S = _S_tensor(s, U.data.dtype, svd_label)
+        if how == "left":
+            return contract(U, S, ["svd_in"], ["svd_out"]), V
+        if how == "right":
+            return U, contract(S, V, ["svd_in"], ["svd_out"])
+        sq = _new(_ops.diag_matrix(torch.sqrt(s), U.data.dtype), list(S.labels))
+        return contract(U, sq, ["svd_in"], ["svd_out"]), contract(sq, V, ["svd_in"], ["svd_out"])
+    mode = 1 if how not in ("left", "right") else 0
+    k = s.shape[0]
+    if how != "right":
+        u2 = U.data.reshape(-1, k).clone()
+        _ops.scale_cols(u2, s, mode)
+        U = _new(u2.reshape(U.data.shape), U.labels)
+    if how != "left":
+        v2 = V.data.reshape(k, -1).clone()
+        _ops.scale_rows(v2, s, mode)
+        V = _new(v2.reshape(V.data.shape), V.labels)
+    return U, V
+
+
+def tensor_svd(tensor, row_labels, svd_label="svd_", absorb_singular_values=None):
+    """``tensor.py:830-959``: SVD of the matricised tensor (rows = the axes
+    in ``row_labels``, in that order).  Returns U, S, V with S the dense
+    diagonal matrix of singular values, or (U, V) with S absorbed."""
+    U, s, V = _svd_parts(tensor, row_labels, svd_label)
+    if absorb_singular_values in ("left", "right", "both"):
+        return _absorb(U, s, V, absorb_singular_values, svd_label)
+    return U, _S_tensor(s, U.data.dtype, svd_label), V
+
+
+_slice_last = _ops.slice_last
+
+
+def truncated_svd(tensor, row_labels, chi=0, threshold=1e-15,
+                  absorb_singular_values="right", absolute=True):
+    """``tensor.py:1112-1182``: keep at most ``chi`` singular values, then
+    those above ``threshold`` (absolute) or ``threshold * s_max``
+    (relative); absorb S ("left", "right", anything else: sqrt into both).
+    Returns (U, V, truncated_evals), or (U, S, V) when absorption is None."""
+    U, s, V = _svd_parts(tensor, row_labels, "svd_")
+    k, _ = _ops.truncation_rank(s, chi, threshold, relative=not absolute)
+    truncated = s[k:]
+    s_keep = s[:k]
+    U = _new(_slice_last(U.data, k), U.labels)
+    V = _new(V.data[0:k], V.labels)
+    if absorb_singular_values is None:
+        return U, _S_tensor(s_keep, U.data.dtype, "svd_"), V
+    how = absorb_singular_values if absorb_singular_values in ("left", "right") else "both"
+    U_new, V_new = _absorb(U, s_keep, V, how, "svd_")
+    return U_new, V_new, truncated
+
+
+def tensor_qr(tensor, row_labels, qr_label="qr_"):
+    """``tensor.py:962-1055``: reduced QR of the matricised tensor."""
+    if not isinstance(row_labels, list):
+        row_labels = [row_labels]
+    t = _new(tensor.data, list(tensor.labels))
+    t.move_indices(row_labels, 0)
+    row_dimension = 1
+    for i, label in enumerate(t.labels):
+        if label not in row_labels:
+            break
+        row_dimension *= t.data.shape[i]
+    column_labels = [x for x in t.labels if x not in row_labels]
+    old_shape = tuple(t.data.shape)
+    ncol = t.data.numel() // row_dimension if row_dimension else 0
+    q, r = _ops.qr(t.data.reshape(row_dimension, ncol))
+    Q = _new(q.reshape(old_shape[0:len(row_labels)] + (q.shape[1],)),
+             row_labels + [qr_label + "in"])
+    R = _new(r.reshape((r.shape[0],) + old_shape[len(row_labels):]),
+             [qr_label + "out"] + column_labels)
+    return Q, R
+
+
+def tensor_lq(tensor, row_labels, lq_label="lq_"):
+    """``tensor.py:1058-1109``: QR on the column labels, relabelled."""
+    col_labels = [x for x in tensor.labels if x not in row_labels]
+    temp_label = lbl.unique_label()
+    Q, L = tensor_qr(tensor, col_labels, qr_label=temp_label)
+    Q.replace_label(temp_label + "in", lq_label + "out")
+    L.replace_label(temp_label + "out", lq_label + "in")
+    return L, Q
+
+
+def conjugate(tensor):
+    """``tensor.py:1185-1190``"""
+    t = tensor.copy()
+    t.conjugate()
+    return t
