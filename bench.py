@@ -1,0 +1,320 @@
+#!/usr/bin/env python
+"""Benchmark: MPO-MPS apply + SVD compression sweeps per second.
+
+Workload (one step = one unit): transverse-field Ising MPO (D=3, J=1, h=0.5)
+on N=64 sites, d=2, applied to a seeded random complex128 MPS with bond
+chi=256 (normalised), the result compressed back to chi=256 by
+``MatrixProductState.svd_compress`` (QR left sweep, truncating SVD right
+sweep) -- tncontract's ``contract_mps_mpo`` + ``svd_compress``.
+
+Arms:
+  (default)          this project on the GPU.  ``value``: sweeps/s with the
+                     input MPS/MPO resident in HBM; ``e2e``: the same through
+                     the public API from pinned host buffers, host->device
+                     copies of the inputs and the device->host read of the
+                     compressed MPS inside the timed region.
+  --impl reference   the reference algorithm on the host cores (the NumPy
+                     restatement in oracle/, same LAPACK calls), on a bounded
+                     sample of the same workload, scaled to sweeps/s by the
+                     algorithmic flop ratio.
+
+Multi-GPU (torchrun): a sweep does not shard; every rank runs its own
+replica (weak scaling) and ``value`` = total sweeps / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SITES, PHYS, MPO_D, CHI = 64, 2, 3, 256
+METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, complex128)"
+# dram bytes (read + write) per tnc_svd call at the workload's bulk shape
+# (512 x 768 complex128), from profiles/svd_jacobi_c128_512x768.txt; None
+# until that capture exists.
+SVD_TRAFFIC_PER_CALL = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--nsites", type=int, default=N_SITES)
+    p.add_argument("--chi", type=int, default=CHI)
+    p.add_argument("--cpu-sample-sites", type=int, default=28)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU legs
+
+
+def cpu_sample(nsites, chi, steps=1):
+    """Reference algorithm (oracle restatement, NumPy/LAPACK) on N=nsites at
+    the full bond dimension; returns (seconds per sample, flops ratio)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import tn_oracle as O
+    from tncontract_gb300 import workloads as W
+    sites = O.random_mps(0, nsites, PHYS, chi, np.complex128, normalise=True)
+    mpo = O.tfim_mpo(nsites)
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        O.apply_compress_sweep(sites, mpo, chi)
+        times.append(time.perf_counter() - t)
+    ratio = W.sweep_flops(nsites, PHYS, MPO_D, chi)["total"] / W.sweep_flops(N_SITES, PHYS, MPO_D, chi)["total"]
+    return times, ratio
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count()
+    cpu_sample(8, 16)  # warm the BLAS threads
+    w = max(args.warmup, 0)
+    if w:
+        cpu_sample(args.cpu_sample_sites, args.chi, steps=1)
+    times, ratio = cpu_sample(args.cpu_sample_sites, args.chi, steps=max(args.steps, 1))
+    per_sweep = statistics.median(times) / ratio
+    value = 1.0 / per_sweep
+    sample = ("apply+svd_compress on N=%d sites at chi=%d (same d, D, dtype), scaled by the "
+              "algorithmic flop ratio %.4f to N=%d" % (args.cpu_sample_sites, args.chi, ratio, N_SITES))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded random MPS, TFIM MPO)",
+            "config": {"workload": "tfim_apply_svd_compress", "nsites": N_SITES, "phys_dim": PHYS,
+                       "mpo_bond": MPO_D, "chi": args.chi, "dtype": "complex128"},
+            "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU leg
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import tncontract_gb300 as tn
+    from tncontract_gb300 import _lib, _ops
+    from tncontract_gb300 import workloads as W
+
+    N, chi = args.nsites, args.chi
+    host_sites = W.random_mps_arrays(0, N, PHYS, chi, np.complex128, normalise=True)
+    host_mpo = W.tfim_mpo_arrays(N)
+    pinned_sites = [torch.from_numpy(a).pin_memory() for a in host_sites]
+    pinned_mpo = [torch.from_numpy(w).pin_memory() for w in host_mpo]
+    h2d = sum(a.nbytes for a in host_sites) + sum(w.nbytes for w in host_mpo)
+
+    psi = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in host_sites])
+    mpo = tn.onedim.MatrixProductOperator([tn.Tensor(w, ["physout", "physin", "left", "right"])
+                                           for w in host_mpo])
+
+    def step():
+        phi = tn.onedim.contract_mps_mpo(psi, mpo)
+        phi.svd_compress(chi=chi)
+        return phi
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(max(args.warmup, 3)):
+        out = step()
+    barrier()
+    launches0 = _lib.kernel_launches()
+    _ops.PROFILE = {}
+    st = torch.cuda.current_stream()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(st)
+        for _ in range(args.steps):
+            out = step()
+        ev1.record(st)
+        barrier()
+    prof = _ops.PROFILE
+    _ops.PROFILE = None
+    launches = _lib.kernel_launches() - launches0
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * args.steps / elapsed
+    summary = _ops.profile_summary(prof)
+    bonds = out.bonddims()
+
+    # fidelity of the compressed state with the uncompressed applied state
+    phi_full = tn.onedim.contract_mps_mpo(psi, mpo)
+    ip = lambda a, b: complex(tn.onedim.inner_product_mps(a, b).item())
+    fid_applied = abs(ip(phi_full, out)) ** 2 / (ip(phi_full, phi_full).real * ip(out, out).real)
+
+    # end to end through the public API from pinned host buffers
+    def e2e_step():
+        p = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in pinned_sites])
+        w = tn.onedim.MatrixProductOperator([tn.Tensor(x, ["physout", "physin", "left", "right"])
+                                             for x in pinned_mpo])
+        phi = tn.onedim.contract_mps_mpo(p, w)
+        phi.svd_compress(chi=chi)
+        return [t.to_numpy() for t in phi]
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = e2e_step()
+    barrier()
+    e2e_el = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_el], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_el = float(t.item())
+    d2h = sum(a.nbytes for a in res)
+    e2e_value = world * args.steps / e2e_el
+
+    # dominant native call and its roofline (algorithmic flops / event time)
+    dom = max(summary.items(), key=lambda kv: kv[1][1])
+    name, (ncalls, ms, flops) = dom
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak, peak_src = float(peaks["bf16_tflops"]), "measured"
+    except Exception:
+        peak, peak_src = 1900.0, "fallback"
+    achieved = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+    roofline = {"bound": "tensor", "kernel": name, "launches": ncalls, "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_src,
+                "traffic": SVD_TRAFFIC_PER_CALL if name == "tnc_svd" else None,
+                "fp64_nominal_tflops": 1.25, "frac_of_fp64_nominal": achieved / 1.25,
+                "note": "FP64 path: runs on the FP64 CUDA-core pipe; frac is against the measured bf16 "
+                        "tensor peak, frac_of_fp64_nominal against GB300's nominal FP64 rate"}
+    share = {k: round(v[1] / sum(x[1] for x in summary.values()), 4) for k, v in summary.items()}
+
+    line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": elapsed / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded random MPS, TFIM MPO)",
+            "config": {"workload": "tfim_apply_svd_compress", "path": "plain FP64 drop-in API",
+                       "nsites": N, "phys_dim": PHYS, "mpo_bond": MPO_D, "chi": chi,
+                       "dtype": "complex128", "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (MPS 134 MB in, 1.2 GB applied MPS per step)"},
+            "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "native_call_share": share,
+            "fidelity_compressed_vs_applied": fid_applied,
+            "bond_dims_mid": bonds[N // 2],
+            "clocks": clk.summary(),
+            "sweep_tflop": W.sweep_flops(N, PHYS, MPO_D, chi)["total"] / 1e12}
+    if rank == 0 and not args.no_cpu_baseline:
+        times, ratio = cpu_sample(args.cpu_sample_sites, chi, steps=1)
+        v = ratio / times[0]
+        line["cpu_baseline"] = {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": "apply+svd_compress on N=%d sites at chi=%d, scaled by the "
+                                          "algorithmic flop ratio %.4f to N=%d" % (
+                                              args.cpu_sample_sites, chi, ratio, N)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

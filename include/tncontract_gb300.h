@@ -51,6 +51,8 @@ enum { TNC_OP_N = 0, TNC_OP_T = 1, TNC_OP_C = 2 /* conj-transpose */, TNC_OP_R =
 
 int tnc_abi_version(void);
 const char *tnc_status_string(int status);
+/* Kernels launched by this library since it was loaded (host counter). */
+unsigned long long tnc_kernel_launches(void);
 
 /* ------------------------------------------------------------ data movement */
 

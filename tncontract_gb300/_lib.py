@@ -30,6 +30,7 @@ _psz = C.POINTER(C.c_size_t)
 SIGNATURES = {
     "tnc_abi_version": [],
     "tnc_status_string": [_int],
+    "tnc_kernel_launches": [],
     "tnc_permute": [_int, _vp, _vp, _int, _pi64, _pint, _int, _vp],
     "tnc_scale": [_int, _i64, _pdbl, _vp, _vp, _int, _vp],
     "tnc_axpby": [_int, _i64, _pdbl, _vp, _pdbl, _vp, _vp],
@@ -51,7 +52,14 @@ SIGNATURES = {
     "tnc_truncation_rank": [_int, _i64, _vp, _i64, _dbl, _int, _vp, _vp, _vp],
 }
 
+RESTYPES = {"tnc_status_string": C.c_char_p, "tnc_kernel_launches": C.c_ulonglong}
+
 _LIB = None
+
+
+def kernel_launches():
+    """Kernels launched by the native library so far (host-side counter)."""
+    return int(lib().tnc_kernel_launches())
 
 
 def header_symbols():
@@ -75,7 +83,7 @@ def lib():
     for name, args in SIGNATURES.items():
         fn = getattr(L, name)
         fn.argtypes = args
-        fn.restype = C.c_char_p if name == "tnc_status_string" else C.c_int
+        fn.restype = RESTYPES.get(name, C.c_int)
     _LIB = L
     return L
 

@@ -64,8 +64,33 @@ def _arr(ctype, seq):
     return (ctype * max(1, len(seq)))(*seq)
 
 
-def _call(name, *args):
-    L.check(name, getattr(L.lib(), name)(*args))
+# When set to a dict, every C-ABI call is bracketed by CUDA events on the
+# current stream: PROFILE[name] -> list of (start, end, algorithmic flops).
+PROFILE = None
+
+
+def _call(name, *args, flops=0.0):
+    fn = getattr(L.lib(), name)
+    prof = PROFILE
+    if prof is None:
+        L.check(name, fn(*args))
+        return
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record()
+    st = fn(*args)
+    e.record()
+    prof.setdefault(name, []).append((s, e, float(flops)))
+    L.check(name, st)
+
+
+def profile_summary(prof):
+    """{name: (launches, total ms, total flops)} after a synchronize."""
+    out = {}
+    for name, recs in prof.items():
+        ms = sum(s.elapsed_time(e) for s, e, _ in recs)
+        out[name] = (len(recs), ms, sum(f for _, _, f in recs))
+    return out
 
 
 def empty(shape, dtype):
@@ -271,7 +296,8 @@ def dot_device(x, y, conj_x=False):
 def gemm(opA, opB, m, n, k, A, lda, B, ldb, Cm, ldc, alpha=1.0, beta=0.0,
          batch=1, sA=0, sB=0, sC=0):
     _call("tnc_gemm", code(Cm.dtype), opA, opB, m, n, k, _pair(alpha), _p(A), lda, sA,
-          _p(B), ldb, sB, _pair(beta), _p(Cm), ldc, sC, batch, _stream())
+          _p(B), ldb, sB, _pair(beta), _p(Cm), ldc, sC, batch, _stream(),
+          flops=2.0 * m * n * k * batch * (4 if is_complex(Cm.dtype) else 1))
     return Cm
 
 
@@ -355,8 +381,10 @@ def svd(M, max_sweeps=0, tol=0.0, check=True, info_out=None):
     _call("tnc_svd_workspace_size", code(dt), m, n, C.byref(sz))
     ws = workspace(sz.value)
     info = torch.empty(4, dtype=torch.int32, device=device())
+    mm, nn = max(m, n), min(m, n)
     _call("tnc_svd", code(dt), m, n, _p(M), n, _p(U), _p(S), _p(VH), int(max_sweeps), float(tol),
-          _p(ws), sz.value, _p(info), _stream())
+          _p(ws), sz.value, _p(info), _stream(),
+          flops=(6.0 * mm * nn * nn + 20.0 * nn ** 3) * (4 if is_complex(dt) else 1))
     if info_out is not None:
         info_out.append(info)
     if check:
@@ -383,7 +411,9 @@ def qr(M, check=True):
     _call("tnc_qr_workspace_size", code(M.dtype), m, n, C.byref(sz))
     ws = workspace(sz.value)
     info = torch.empty(1, dtype=torch.int32, device=device())
-    _call("tnc_qr", code(M.dtype), m, n, _p(M), n, _p(Q), _p(R), _p(ws), sz.value, _p(info), _stream())
+    mm, nn = max(m, n), min(m, n)
+    _call("tnc_qr", code(M.dtype), m, n, _p(M), n, _p(Q), _p(R), _p(ws), sz.value, _p(info), _stream(),
+          flops=(2.0 * mm * nn * nn - 2.0 / 3.0 * nn ** 3) * (4 if is_complex(M.dtype) else 1))
     if check:
         st = int(info.item())
         if st != L.OK:

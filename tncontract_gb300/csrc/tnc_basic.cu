@@ -7,6 +7,8 @@
 
 namespace tnc {
 
+unsigned long long g_tnc_launches = 0;
+
 // ------------------------------------------------------------------ permute
 struct PermParams {
   int rank;             // after merging, >= 1
@@ -352,6 +354,8 @@ extern "C" {
 
 int tnc_abi_version(void) { return 1; }
 
+unsigned long long tnc_kernel_launches(void) { return __atomic_load_n(&g_tnc_launches, __ATOMIC_RELAXED); }
+
 const char* tnc_status_string(int s) {
   switch (s) {
     case TNC_OK: return "ok";
@@ -412,7 +416,7 @@ int tnc_nrm2(int dtype, int64_t n, const void* x, double* out, void* stream) {
     TNC_DISPATCH(dtype, T, sumsq_kernel<T><<<grid1d(n, 256, 152 * 4), 256, 0, st>>>(n, (const T*)x, out));
   }
   sqrt_inplace<<<1, 1, 0, st>>>(out);
-  return launch_status();
+  return launch_status(n > 0 ? 2 : 1);
 }
 
 int tnc_dot(int dtype, int64_t n, const void* x, const void* y, int conj_x, double* out, void* stream) {

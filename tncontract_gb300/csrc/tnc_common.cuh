@@ -140,7 +140,12 @@ inline int elem_size(int dtype) {
   }
 }
 
-inline int launch_status() {
+// Number of kernels this library has launched (tnc_kernel_launches()).
+extern unsigned long long g_tnc_launches;
+
+// Record `n` kernel launches just issued and report the launch status.
+inline int launch_status(int n = 1) {
+  __atomic_fetch_add(&g_tnc_launches, (unsigned long long)n, __ATOMIC_RELAXED);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TNC_OK : TNC_ERR_CUDA;
 }

@@ -204,7 +204,7 @@ static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, vo
   if (gq > 152 * 16) gq = 152 * 16;
   qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
   qr_extract_r<T><<<grid1d(k * n, 256), 256, 0, st>>>(Bt, m, n, k, R);
-  if (launch_status()) return TNC_ERR_CUDA;
+  if (launch_status(4)) return TNC_ERR_CUDA;  // factor, error copy, form Q, extract R
   // Q = Qt^T
   int64_t shp[2] = {k, m};
   int perm[2] = {1, 0};

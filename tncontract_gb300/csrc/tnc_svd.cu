@@ -255,7 +255,8 @@ static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typenam
   row_norms_kernel<T><<<grid1d(nr * 32, 256), 256, 0, st>>>(W, nr, L, D, info);
   rank_kernel<R><<<grid1d(nr, 128), 128, 0, st>>>(D, nr, pos);
   svd_output_kernel<T><<<grid1d(nr * L, 256), 256, 0, st>>>(W, J, D, pos, nr, L, tall, U, S, VH);
-  return launch_status();
+  // [jacobi], error copy, row norms, rank, output
+  return launch_status(nr > 1 ? 5 : 4);
 }
 
 }  // namespace tnc
