@@ -53,7 +53,60 @@ def parse():
     p.add_argument("--chi", type=int, default=CHI)
     p.add_argument("--cpu-sample-sites", type=int, default=28)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--micro", default=None,
+                   help="time one native op instead: svd:MxN:DT, qr:MxN:DT or gemm:MxNxK:DT "
+                        "(DT in f32,f64,c64,c128); used for kernel profiling")
     return p.parse_args()
+
+
+def run_micro(args):
+    """One native op at a fixed shape, timed with CUDA events (3 warm-up calls)."""
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from tncontract_gb300 import _ops
+    op, shape, dt = args.micro.split(":")
+    dims = [int(x) for x in shape.split("x")]
+    npdt = {"f32": np.float32, "f64": np.float64, "c64": np.complex64, "c128": np.complex128}[dt]
+    rng = np.random.default_rng(0)
+
+    def mat(r, c):
+        a = rng.standard_normal((r, c))
+        if np.iscomplexobj(np.zeros(0, npdt)):
+            a = a + 1j * rng.standard_normal((r, c))
+        return torch.from_numpy(a.astype(npdt)).cuda()
+
+    infos = []
+    if op == "svd":
+        A = mat(*dims)
+        fn = lambda: _ops.svd(A, check=False, info_out=infos)
+    elif op == "qr":
+        A = mat(*dims)
+        fn = lambda: _ops.qr(A, check=False)
+    elif op == "gemm":
+        A, B = mat(dims[0], dims[2]), mat(dims[2], dims[1])
+        fn = lambda: _ops.matmul(A, B)
+    else:
+        raise SystemExit("unknown micro op " + op)
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    _ops.PROFILE = {}
+    for _ in range(max(args.steps, 1)):
+        fn()
+    torch.cuda.synchronize()
+    summ = _ops.profile_summary(_ops.PROFILE)
+    _ops.PROFILE = None
+    name = {"svd": "tnc_svd", "qr": "tnc_qr", "gemm": "tnc_gemm"}[op]
+    n, ms, fl = summ[name]
+    extra = {}
+    if infos:
+        st, sweeps, last = (int(v) for v in infos[-1][:3].cpu())
+        extra = {"status": st, "jacobi_sweeps": sweeps}
+    print(json.dumps(dict({"micro": args.micro, "calls": n, "ms_per_call": ms / n,
+                           "algorithmic_tflops": fl / (ms / 1e3) / 1e12}, **extra)), flush=True)
+    return 0
 
 
 # ------------------------------------------------------------------ clocks
@@ -311,6 +364,8 @@ def run_ours(args):
 
 def main():
     args = parse()
+    if args.micro:
+        return run_micro(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

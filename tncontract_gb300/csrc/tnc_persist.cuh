@@ -89,6 +89,105 @@ template <> __device__ __forceinline__ void stcg<c128>(c128* p, c128 v) {
   __stcg(reinterpret_cast<double2*>(p), make_double2(v.re, v.im));
 }
 
+// ---------------------------------------------------------------- warp vector ops
+// Vectors live in L2 (other CTAs update them between steps).  Each lane
+// issues kChunk independent loads before using any of them, so a pass over a
+// vector costs a few L2 round trips instead of one per element.
+template <typename T> struct chunk { static constexpr int U = sizeof(T) >= 16 ? 4 : 8; };
+
+// a = |x|^2, b = |y|^2, g = sum_k x_k conj(y_k) over one warp (all lanes get them)
+template <typename T>
+__device__ __forceinline__ void warp_pair_dots(const T* x, const T* y, int64_t L,
+                                               typename traits<T>::real& a, typename traits<T>::real& b, T& g) {
+  typedef typename traits<T>::real R;
+  constexpr int U = chunk<T>::U;
+  const int lane = threadIdx.x & 31;
+  R a_ = 0, b_ = 0;
+  T g_ = zero_<T>();
+  for (int64_t base = 0; base < L; base += 32 * U) {
+    T xv[U], yv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = base + u * 32 + lane;
+      xv[u] = (k < L) ? ldcg(x + k) : zero_<T>();
+      yv[u] = (k < L) ? ldcg(y + k) : zero_<T>();
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      a_ += abs2_(xv[u]);
+      b_ += abs2_(yv[u]);
+      fma_(g_, xv[u], conj_(yv[u]));
+    }
+  }
+  a = warp_sum(a_);
+  b = warp_sum(b_);
+  g = warp_sum(g_);
+}
+
+// x' = c x - se y, y' = sec x + c y over one warp
+template <typename T>
+__device__ __forceinline__ void warp_pair_rotate(T* x, T* y, int64_t L, typename traits<T>::real c, T se, T sec) {
+  constexpr int U = chunk<T>::U;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = 0; base < L; base += 32 * U) {
+    T xv[U], yv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = base + u * 32 + lane;
+      if (k < L) { xv[u] = ldcg(x + k); yv[u] = ldcg(y + k); }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = base + u * 32 + lane;
+      if (k < L) {
+        stcg(x + k, c * xv[u] - se * yv[u]);
+        stcg(y + k, sec * xv[u] + c * yv[u]);
+      }
+    }
+  }
+}
+
+// w = sum_{k >= c} conj(v_k) col_k with v_c = 1 (v in L2, col owned by the warp)
+template <typename T>
+__device__ __forceinline__ T warp_reflector_dot(const T* v, const T* col, int64_t c, int64_t m) {
+  constexpr int U = chunk<T>::U;
+  const int lane = threadIdx.x & 31;
+  T w = (lane == 0) ? col[c] : zero_<T>();
+  for (int64_t base = c + 1; base < m; base += 32 * U) {
+    T vv[U], cv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = base + u * 32 + lane;
+      vv[u] = (k < m) ? ldcg(v + k) : zero_<T>();
+      cv[u] = (k < m) ? col[k] : zero_<T>();
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) fma_(w, conj_(vv[u]), cv[u]);
+  }
+  return warp_sum(w);
+}
+
+// col_k -= f v_k for k >= c (v_c = 1)
+template <typename T>
+__device__ __forceinline__ void warp_reflector_axpy(const T* v, T* col, T f, int64_t c, int64_t m) {
+  constexpr int U = chunk<T>::U;
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) col[c] = col[c] - f;
+  for (int64_t base = c + 1; base < m; base += 32 * U) {
+    T vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = base + u * 32 + lane;
+      vv[u] = (k < m) ? ldcg(v + k) : zero_<T>();
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t k = base + u * 32 + lane;
+      if (k < m) col[k] = col[k] - f * vv[u];
+    }
+  }
+}
+
 // info[0] = first error recorded by the persistent launch (0 = none)
 static __global__ void copy_sync_error(const SyncWords* sw, int* info) {
   int e = sw->err;

@@ -64,13 +64,9 @@ __device__ void make_reflector(T* col, int64_t c, int64_t m, T* tau_out) {
 // col[i] -= conj(tau) * (v^H col) * v[i], i >= c  (applies H_c^H)
 template <typename T>
 __device__ __forceinline__ void apply_reflector_h(T* col, const T* v, T tau, int64_t c, int64_t m) {
-  const int lane = threadIdx.x & 31;
-  T w = (lane == 0) ? col[c] : zero_<T>();
-  for (int64_t i = c + 1 + lane; i < m; i += 32) fma_(w, conj_(ldcg(v + i)), col[i]);
-  w = warp_sum(w);
-  T f = conj_(tau) * w;
-  if (lane == 0) col[c] = col[c] - f;
-  for (int64_t i = c + 1 + lane; i < m; i += 32) col[i] = col[i] - f * ldcg(v + i);
+  const T w = warp_reflector_dot(v, col, c, m);
+  __syncwarp();
+  warp_reflector_axpy(v, col, conj_(tau) * w, c, m);
   __syncwarp();
 }
 
@@ -121,13 +117,9 @@ qr_form_q_kernel(const T* __restrict__ Bt, int64_t m, int64_t k, const T* __rest
       const T* v = Bt + c * m;
       const T tc = tau[c];
       // q -= tau * (v^H q) * v  (H_c, not conjugated)
-      T w = (lane == 0) ? q[c] : zero_<T>();
-      for (int64_t i = c + 1 + lane; i < m; i += 32) fma_(w, conj_(v[i]), q[i]);
-      w = warp_sum(w);
-      T f = tc * w;
+      const T w = warp_reflector_dot(v, q, c, m);
       __syncwarp();
-      if (lane == 0) q[c] = q[c] - f;
-      for (int64_t i = c + 1 + lane; i < m; i += 32) q[i] = q[i] - f * v[i];
+      warp_reflector_axpy(v, q, tc * w, c, m);
       __syncwarp();
     }
   }

@@ -56,17 +56,9 @@ jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, uns
         if (p >= nr || q >= nr) continue;
         T* x = W + p * L;
         T* y = W + q * L;
-        R a = 0, b = 0;
-        T g = zero_<T>();
-        for (int64_t k = lane; k < L; k += 32) {
-          T xv = ldcg(x + k), yv = ldcg(y + k);
-          a += abs2_(xv);
-          b += abs2_(yv);
-          fma_(g, xv, conj_(yv));
-        }
-        a = warp_sum(a);
-        b = warp_sum(b);
-        g = warp_sum(g);
+        R a, b;
+        T g;
+        warp_pair_dots(x, y, L, a, b, g);
         const R h = sqrt(abs2_(g));
         if (!(h > rtol * sqrt(a) * sqrt(b))) continue;  // also skips NaN / zero rows
         const R tau = (b - a) / (2 * h);
@@ -77,18 +69,8 @@ jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, uns
         const R s = c * t;
         const T e = g * (R(1) / h);
         const T se = s * e, sec = s * conj_(e);
-        for (int64_t k = lane; k < L; k += 32) {
-          T xv = ldcg(x + k), yv = ldcg(y + k);
-          stcg(x + k, c * xv - se * yv);
-          stcg(y + k, sec * xv + c * yv);
-        }
-        T* xj = J + p * nr;
-        T* yj = J + q * nr;
-        for (int64_t k = lane; k < nr; k += 32) {
-          T xv = ldcg(xj + k), yv = ldcg(yj + k);
-          stcg(xj + k, c * xv - se * yv);
-          stcg(yj + k, sec * xv + c * yv);
-        }
+        warp_pair_rotate(x, y, L, c, se, sec);
+        if (J != nullptr) warp_pair_rotate(J + p * nr, J + q * nr, nr, c, se, sec);
         ++rot;
       }
       if (!grid_barrier(sw, gridDim.x)) return;
