@@ -43,7 +43,8 @@ enum {
   TNC_ERR_NONFINITE = 3,     /* NaN / Inf met in the input                 */
   TNC_ERR_CUDA = 4,          /* a CUDA launch or API call failed           */
   TNC_ERR_WORKSPACE = 5,     /* workspace smaller than *_workspace_size    */
-  TNC_ERR_TIMEOUT = 6        /* a bounded device-side wait gave up         */
+  TNC_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up         */
+  TNC_ERR_TOO_LARGE = 7      /* problem exceeds tnc_svd_noalloc's scratch  */
 };
 
 /* matrix operation applied to a row-major operand */
@@ -166,6 +167,22 @@ int tnc_svd_workspace_size(int dtype, int64_t m, int64_t n, size_t *bytes);
 int tnc_svd(int dtype, int64_t m, int64_t n, const void *A, int64_t lda,
             void *U, void *S, void *VH, int max_sweeps, double tol,
             void *work, size_t work_bytes, int *info, void *stream);
+
+/* tnc_svd for callers that cannot provide a workspace.  No counterpart in the
+ * reference: it exists for hosts where this library may not allocate and
+ * the caller has no spare buffer to lend it (a plugin inside another
+ * framework that owns the whole device-memory budget, a service that
+ * reserves all memory at start-up).  The work area is a fixed 16 MiB
+ * array inside the library image (held by every GPU that loads the library
+ * until exit); problems whose tnc_svd_workspace_size exceeds it return
+ * TNC_ERR_TOO_LARGE.  Same arguments and results as tnc_svd otherwise.  All
+ * calls on a device share that area: calls that overlap on the GPU race, so
+ * order them on one stream.  The first call on a device looks up the area's
+ * device address (with that device current); make it before any stream
+ * capture. */
+int tnc_svd_noalloc(int dtype, int64_t m, int64_t n, const void *A,
+                    int64_t lda, void *U, void *S, void *VH, int max_sweeps,
+                    double tol, int *info, void *stream);
 
 /* Truncation decision on descending singular values S (n, real type of
  * dtype): k = #{ s_i > t } capped at chi (chi <= 0: no cap), t = threshold

@@ -14,7 +14,7 @@ from . import _build
 
 # C-ABI constants (include/tncontract_gb300.h)
 F32, F64, C64, C128 = 0, 1, 2, 3
-OK, ERR_ARG, ERR_NOT_CONVERGED, ERR_NONFINITE, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT = range(7)
+OK, ERR_ARG, ERR_NOT_CONVERGED, ERR_NONFINITE, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_TOO_LARGE = range(8)
 OP_N, OP_T, OP_C, OP_R = 0, 1, 2, 3
 
 _vp = C.c_void_p
@@ -50,6 +50,7 @@ SIGNATURES = {
     "tnc_svd_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_svd": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, C.c_size_t, _vp, _vp],
     "tnc_truncation_rank": [_int, _i64, _vp, _i64, _dbl, _int, _vp, _vp, _vp],
+    "tnc_svd_noalloc": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, _vp],
 }
 
 RESTYPES = {"tnc_status_string": C.c_char_p, "tnc_kernel_launches": C.c_ulonglong}

@@ -365,6 +365,7 @@ const char* tnc_status_string(int s) {
     case TNC_ERR_CUDA: return "CUDA error";
     case TNC_ERR_WORKSPACE: return "workspace too small";
     case TNC_ERR_TIMEOUT: return "device-side wait timed out";
+    case TNC_ERR_TOO_LARGE: return "problem needs more than the fixed scratch of tnc_svd_noalloc (16 MiB)";
     default: return "unknown status";
   }
 }

@@ -261,3 +261,68 @@ extern "C" int tnc_svd(int dtype, int64_t m, int64_t n, const void* A, int64_t l
                                   tol, work, work_bytes, info, st));
   return TNC_ERR_ARG;
 }
+
+// ---------------------------------------------------------------------------
+// SVD without any device allocation by the caller.
+//
+// Some callers cannot hand this library a workspace: a plugin hosted inside
+// another framework's process that owns the whole device-memory budget
+// through its own allocator, or a service that reserves all its memory at
+// start-up and forbids allocations afterwards.  For them the SVD below uses a
+// fixed scratch area that lives in the library image itself (a file-scope
+// __device__ array): every GPU that loads the library holds these bytes until
+// the process exits, and no call allocates or frees device memory.
+//
+// Limit: the problem's workspace (tnc_svd_workspace_size) must fit in
+// kNoAllocScratchBytes = 16 MiB, e.g. complex128 up to 512 x 768 or
+// complex64 up to 768 x 1024; larger problems are rejected with
+// TNC_ERR_TOO_LARGE before anything is launched.
+//
+// All calls on a device share the one scratch area and it keeps whatever the
+// previous call left there; the SVD initialises every part it reads (working
+// copy, rotation accumulator, counters, barrier words) at the start of each
+// call.  Calls whose work overlaps on the GPU (different streams, or
+// different host threads without ordering) race on the shared scratch: order
+// them on one stream.
+//
+// The device address of the scratch is looked up once per device, with that
+// device current, on the first call made on it (cudaGetSymbolAddress); make
+// that first call before any stream capture.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace tnc {
+
+static constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_svd_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[128] = {nullptr};  // device address per device ordinal
+
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TNC_ERR_CUDA;
+  if (dev < 0 || dev >= 128) return TNC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_svd_scratch) != cudaSuccess || p == nullptr) return TNC_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return TNC_OK;
+}
+
+}  // namespace tnc
+
+extern "C" int tnc_svd_noalloc(int dtype, int64_t m, int64_t n, const void* A, int64_t lda, void* U, void* S,
+                               void* VH, int max_sweeps, double tol, int* info, void* stream) {
+  size_t need = 0;
+  int s = tnc_svd_workspace_size(dtype, m, n, &need);
+  if (s != TNC_OK) return s;
+  if (need > tnc::kNoAllocScratchBytes) return TNC_ERR_TOO_LARGE;
+  void* scratch = nullptr;
+  s = tnc::noalloc_scratch(&scratch);
+  if (s != TNC_OK) return s;
+  return tnc_svd(dtype, m, n, A, lda, U, S, VH, max_sweeps, tol, scratch, tnc::kNoAllocScratchBytes, info, stream);
+}
