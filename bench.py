@@ -37,10 +37,10 @@ sys.path.insert(0, ROOT)
 
 N_SITES, PHYS, MPO_D, CHI = 64, 2, 3, 256
 METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, complex128)"
-# dram bytes (read + write) per tnc_svd call at the workload's bulk shape
-# (512 x 768 complex128), from profiles/svd_jacobi_c128_512x768.txt; None
-# until that capture exists.
-SVD_TRAFFIC_PER_CALL = None
+# dram bytes (read + write) per call of the dominant native op at the
+# workload's bulk shape, from the ncu summaries in profiles/; absent = not
+# captured.
+TRAFFIC_PER_CALL = {}
 
 
 def parse():
@@ -53,6 +53,9 @@ def parse():
     p.add_argument("--chi", type=int, default=CHI)
     p.add_argument("--cpu-sample-sites", type=int, default=28)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--batch", type=int, default=8, help="independent instances per GPU")
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 drop-in comparison")
     p.add_argument("--micro", default=None,
                    help="time one native op instead: svd:MxN:DT, qr:MxN:DT or gemm:MxNxK:DT "
                         "(DT in f32,f64,c64,c128); used for kernel profiling")
@@ -87,6 +90,14 @@ def run_micro(args):
     elif op == "gemm":
         A, B = mat(dims[0], dims[2]), mat(dims[2], dims[1])
         fn = lambda: _ops.matmul(A, B)
+    elif op.startswith("svdrows"):
+        A = mat(*dims)
+        h = int(op[7:]) if len(op) > 7 else None
+
+        def fn():
+            r = _ops.svd_rows(A, block_rows=h)
+            infos.append(r[3])
+            return r
     else:
         raise SystemExit("unknown micro op " + op)
     for _ in range(3):
@@ -98,7 +109,7 @@ def run_micro(args):
     torch.cuda.synchronize()
     summ = _ops.profile_summary(_ops.PROFILE)
     _ops.PROFILE = None
-    name = {"svd": "tnc_svd", "qr": "tnc_qr", "gemm": "tnc_gemm"}[op]
+    name = {"svd": "tnc_svd", "qr": "tnc_qr", "gemm": "tnc_gemm"}.get(op, "tnc_svd_rows")
     n, ms, fl = summ[name]
     extra = {}
     if infos:
@@ -235,30 +246,39 @@ def run_ours(args):
     __graft_entry__.build()
     import tncontract_gb300 as tn
     from tncontract_gb300 import _lib, _ops
+    from tncontract_gb300 import engine as E
     from tncontract_gb300 import workloads as W
 
-    N, chi = args.nsites, args.chi
-    host_sites = W.random_mps_arrays(0, N, PHYS, chi, np.complex128, normalise=True)
+    N, chi, B = args.nsites, args.chi, args.batch
+    warm = max(args.warmup, 3)
+    # instance b of rank r uses seed (r * B + b); every instance is a full workload
+    host_batch = [W.random_mps_arrays(rank * B + b, N, PHYS, chi, np.complex128, normalise=True)
+                  for b in range(B)]
     host_mpo = W.tfim_mpo_arrays(N)
-    pinned_sites = [torch.from_numpy(a).pin_memory() for a in host_sites]
-    pinned_mpo = [torch.from_numpy(w).pin_memory() for w in host_mpo]
-    h2d = sum(a.nbytes for a in host_sites) + sum(w.nbytes for w in host_mpo)
+    dt = E.compute_dtype(args.precision, True)
+    np_dt = np.complex64 if dt == torch.complex64 else np.complex128
+    # FP32 storage needs balanced sites (see engine.balance); the log norms
+    # travel with the host buffers
+    balanced = [E.balance(sites) for sites in host_batch]
+    log_norms = [ln for _, ln in balanced]
+    pinned_batch = [[torch.from_numpy(a.astype(np_dt)).pin_memory() for a in sites] for sites, _ in balanced]
+    pinned_mpo = [torch.from_numpy(w.astype(np_dt)).pin_memory() for w in host_mpo]
+    h2d = sum(a.numel() * a.element_size() for sites in pinned_batch for a in sites) + \
+        sum(w.numel() * w.element_size() for w in pinned_mpo)
 
-    psi = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in host_sites])
-    mpo = tn.onedim.MatrixProductOperator([tn.Tensor(w, ["physout", "physin", "left", "right"])
-                                           for w in host_mpo])
+    dev_batch = [E.to_sites(sites, dt) for sites in pinned_batch]
+    dev_mpo = E.to_sites(pinned_mpo, dt)
+    streams = [torch.cuda.Stream() for _ in range(B)]
 
     def step():
-        phi = tn.onedim.contract_mps_mpo(psi, mpo)
-        phi.svd_compress(chi=chi)
-        return phi
+        return E.apply_compress_batch(dev_batch, dev_mpo, chi, streams=streams, log_norms=log_norms)
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(warm):
         out = step()
     barrier()
     launches0 = _lib.kernel_launches()
@@ -281,23 +301,15 @@ def run_ours(args):
         t = torch.tensor([elapsed], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
-    value = world * args.steps / elapsed
+    value = world * B * args.steps / elapsed
     summary = _ops.profile_summary(prof)
-    bonds = out.bonddims()
 
-    # fidelity of the compressed state with the uncompressed applied state
-    phi_full = tn.onedim.contract_mps_mpo(psi, mpo)
-    ip = lambda a, b: complex(tn.onedim.inner_product_mps(a, b).item())
-    fid_applied = abs(ip(phi_full, out)) ** 2 / (ip(phi_full, phi_full).real * ip(out, out).real)
-
-    # end to end through the public API from pinned host buffers
+    # end to end through the public API: pinned host arrays in, host arrays out
     def e2e_step():
-        p = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in pinned_sites])
-        w = tn.onedim.MatrixProductOperator([tn.Tensor(x, ["physout", "physin", "left", "right"])
-                                             for x in pinned_mpo])
-        phi = tn.onedim.contract_mps_mpo(p, w)
-        phi.svd_compress(chi=chi)
-        return [t.to_numpy() for t in phi]
+        sites = [E.to_sites(s, dt) for s in pinned_batch]
+        mpo = E.to_sites(pinned_mpo, dt)
+        res = E.apply_compress_batch(sites, mpo, chi, streams=streams, log_norms=log_norms)
+        return [[t.cpu().numpy() for t in r] for r in res]
 
     e2e_step()
     barrier()
@@ -310,44 +322,73 @@ def run_ours(args):
         t = torch.tensor([e2e_el], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_el = float(t.item())
-    d2h = sum(a.nbytes for a in res)
-    e2e_value = world * args.steps / e2e_el
+    d2h = sum(a.nbytes for r in res for a in r)
+    e2e_value = world * B * args.steps / e2e_el
 
-    # dominant native call and its roofline (algorithmic flops / event time)
+    # plain FP64 drop-in path (this project's straightforward FP64 method) on
+    # instance 0, and the fidelity error of the measured path against it
+    extra = {}
+    if rank == 0 and not args.no_plain:
+        psi = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in host_batch[0]])
+        mpo = tn.onedim.MatrixProductOperator([tn.Tensor(w, ["physout", "physin", "left", "right"])
+                                               for w in host_mpo])
+
+        def plain():
+            phi = tn.onedim.contract_mps_mpo(psi, mpo)
+            phi.svd_compress(chi=chi)
+            return phi
+
+        plain()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ref = plain()
+        torch.cuda.synchronize()
+        t_plain = time.perf_counter() - t0
+        ref_sites = []
+        for t in ref:
+            lab = t.labels
+            ref_sites.append(_ops.permute(t.data, [lab.index(ref.phys_label), lab.index(ref.left_label),
+                                                   lab.index(ref.right_label)]))
+        fid = E.fidelity(ref_sites, [_ops.cast(x, torch.complex128) for x in out[0]])
+        extra = {"plain_fp64_sweeps_per_s": 1.0 / t_plain,
+                 "speedup_vs_plain_fp64": value / (1.0 / t_plain),
+                 "fidelity_error_vs_plain_fp64": 1.0 - fid}
+
     dom = max(summary.items(), key=lambda kv: kv[1][1])
     name, (ncalls, ms, flops) = dom
-    peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         peak, peak_src = float(peaks["bf16_tflops"]), "measured"
     except Exception:
         peak, peak_src = 1900.0, "fallback"
     achieved = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+    fp_note = ("FP32 CUDA-core arithmetic (Jacobi rotations, Householder); frac is against the "
+               "measured bf16 tensor peak, frac_of_fp32_nominal against GB300's nominal FP32 rate "
+               "(152 SMs x 128 FMA x 2 x 2.07 GHz = 80.5 TFLOP/s)")
     roofline = {"bound": "tensor", "kernel": name, "launches": ncalls, "achieved": achieved,
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_src,
-                "traffic": SVD_TRAFFIC_PER_CALL if name == "tnc_svd" else None,
-                "fp64_nominal_tflops": 1.25, "frac_of_fp64_nominal": achieved / 1.25,
-                "note": "FP64 path: runs on the FP64 CUDA-core pipe; frac is against the measured bf16 "
-                        "tensor peak, frac_of_fp64_nominal against GB300's nominal FP64 rate"}
-    share = {k: round(v[1] / sum(x[1] for x in summary.values()), 4) for k, v in summary.items()}
+                "traffic": TRAFFIC_PER_CALL.get(name), "fp32_nominal_tflops": 80.5,
+                "frac_of_fp32_nominal": achieved / 80.5, "note": fp_note}
+    tot_ms = sum(x[1] for x in summary.values())
+    share = {k: round(v[1] / tot_ms, 4) for k, v in summary.items() if v[1] / tot_ms > 1e-4}
 
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": elapsed / args.steps * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "warmup": warm, "ms_per_step": elapsed / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64" if dt == torch.complex64 else "c128",
             "data": "synthetic (seeded random MPS, TFIM MPO)",
-            "config": {"workload": "tfim_apply_svd_compress", "path": "plain FP64 drop-in API",
-                       "nsites": N, "phys_dim": PHYS, "mpo_bond": MPO_D, "chi": chi,
-                       "dtype": "complex128", "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2 (MPS 134 MB in, 1.2 GB applied MPS per step)"},
-            "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
+            "config": {"workload": "tfim_apply_svd_compress", "path": "engine (%s)" % args.precision,
+                       "batch_per_gpu": B, "nsites": N, "phys_dim": PHYS, "mpo_bond": MPO_D, "chi": chi,
+                       "input_dtype": "complex128", "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2 (%d MPS of 134 MB in, 1.2 GB applied each)" % B},
+            "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d // 1,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": roofline,
             "native_call_share": share,
-            "fidelity_compressed_vs_applied": fid_applied,
-            "bond_dims_mid": bonds[N // 2],
             "clocks": clk.summary(),
             "sweep_tflop": W.sweep_flops(N, PHYS, MPO_D, chi)["total"] / 1e12}
+    line.update(extra)
     if rank == 0 and not args.no_cpu_baseline:
         times, ratio = cpu_sample(args.cpu_sample_sites, chi, steps=1)
         v = ratio / times[0]

@@ -96,7 +96,8 @@ int tnc_trace(int dtype, int rank, const int64_t *shape, int axis1, int axis2,
               const void *src, void *dst, void *stream);
 
 /* A[i, :] *= f(d[i]) for a rows x cols row-major A (lda), d real (float for
- * F32/C64, double for F64/C128), f = identity (mode 0) or sqrt (mode 1).
+ * F32/C64, double for F64/C128), f = identity (mode 0), sqrt (mode 1),
+ * 1/x (mode 2) or 1/x^2 (mode 3; zero stays zero).
  * Replaces the dense diag(S) contractions that absorb singular values
  * (tensor.py:940-959, 1166-1182; onedim_core.py:347-351). */
 int tnc_scale_rows(int dtype, int64_t rows, int64_t cols, const void *d,
@@ -183,6 +184,33 @@ int tnc_svd(int dtype, int64_t m, int64_t n, const void *A, int64_t lda,
 int tnc_svd_noalloc(int dtype, int64_t m, int64_t n, const void *A,
                     int64_t lda, void *U, void *S, void *VH, int max_sweeps,
                     double tol, int *info, void *stream);
+
+/* Jacobi stage of the truncating sweep SVD (left_canonise's SVD branch,
+ * onedim_core.py:317-343): the rows of W = A (m <= n) or A^H (m > n),
+ * min(m,n) x max(m,n), are made mutually orthogonal by one-sided Jacobi
+ * rotations that are not accumulated (block ordering: half-blocks of rows
+ * in registers and shared memory, one cooperative launch).  Writes W (caller
+ * buffer), S = row norms sorted descending (real type of dtype) and order
+ * (int64: order[i] = row of W holding the i-th singular triplet).  For a wide
+ * A, rows order[:k] of W are S_k V_k^H and U_k = A (S_k V_k^H)^H S_k^-2; for
+ * a tall A they are S_k U_k^H and S_k V_k^H = U_k^H A.  block_rows (2, 4, 8
+ * or 16; anything else selects 8) is the half-block height, chosen per shape
+ * by the caller's autotuner.  max(m,n) <= 1024
+ * (512 for F64/C128).  info as for tnc_svd. */
+int tnc_svd_rows_workspace_size(int dtype, int64_t m, int64_t n, size_t *bytes);
+int tnc_svd_rows(int dtype, int64_t m, int64_t n, const void *A, void *W,
+                 void *S, int64_t *order, int max_sweeps, double tol,
+                 int block_rows, void *work, size_t work_bytes, int *info,
+                 void *stream);
+
+/* dst <- rows order[0:k] of src (row length L), k read from device memory
+ * (capped by kmax): mode 0 copies rows (dst k x L); mode 1 writes
+ * dst[c][i] = conj(src[order[i]][c]) / S[i] (dst L x k, leading dim k).
+ * The slicing U.data[:, :, :k] / V.data[:k] of onedim_core.py:340-343 on the
+ * Jacobi output. */
+int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
+                    const int64_t *k, int64_t kmax, const void *S, int mode,
+                    void *dst, void *stream);
 
 /* Truncation decision on descending singular values S (n, real type of
  * dtype): k = #{ s_i > t } capped at chi (chi <= 0: no cap), t = threshold

@@ -38,12 +38,52 @@ def _qr(M):
     return torch.from_numpy(q), torch.from_numpy(r)
 
 
-def _trunc(S, chi, threshold, relative):
+def _trunc(S, chi, threshold, relative, with_smax=False, kdev_out=None):
     s = S.numpy()
     keep = s[:chi] if chi else s
     thr = s[0] * threshold if relative else threshold
     k = int(np.count_nonzero(keep > thr))
-    return k, float(np.sum(s[k:].astype(np.float64) ** 2))
+    if kdev_out is not None:
+        kdev_out.append(torch.tensor([k], dtype=torch.int64))
+    disc = float(np.sum(s[k:].astype(np.float64) ** 2))
+    if with_smax:
+        return k, disc, float(s[0]) if s.size else 0.0
+    return k, disc
+
+
+def _strided(t, off, rows, cols, ld):
+    return torch.as_strided(t, (rows, cols), (ld, 1), t.storage_offset() + off)
+
+
+def _gemm(opA, opB, m, n, k, A, lda, B, ldb, Cm, ldc, alpha=1.0, beta=0.0, batch=1, sA=0, sB=0, sC=0):
+    ops_ = {0: lambda x: x, 1: lambda x: x.T, 2: lambda x: x.conj().T, 3: lambda x: x.conj()}
+    a_shape = (k, m) if opA in (1, 2) else (m, k)
+    b_shape = (n, k) if opB in (1, 2) else (k, n)
+    for b in range(batch):
+        a = ops_[opA](_strided(A, b * sA, a_shape[0], a_shape[1], lda))
+        bb = ops_[opB](_strided(B, b * sB, b_shape[0], b_shape[1], ldb))
+        c = _strided(Cm, b * sC, m, n, ldc)
+        r = complex(alpha) * (a @ bb) if Cm.is_complex() else float(complex(alpha).real) * (a @ bb)
+        if complex(beta) != 0:
+            r = r + (complex(beta) if Cm.is_complex() else complex(beta).real) * c
+        c.copy_(r)
+    return Cm
+
+
+def _svd_rows(M, max_sweeps=0, tol=0.0):
+    m, n = M.shape
+    u, s, vh = np.linalg.svd(M.numpy(), full_matrices=False)
+    W = s[:, None] * vh if m <= n else s[:, None] * np.conj(u).T
+    return (torch.from_numpy(np.ascontiguousarray(W)), torch.from_numpy(s),
+            torch.arange(len(s), dtype=torch.int64), torch.zeros(4, dtype=torch.int32))
+
+
+def _gather(W, order, kdev, kmax, S=None, mode=0):
+    k = min(int(kdev.reshape(-1)[0]), kmax)
+    rows = W[order[:k]]
+    if mode == 0:
+        return rows.contiguous()
+    return (rows.conj().T / S[:k].to(W.dtype)[None, :]).contiguous()
 
 
 def _copy2d(src, rows, cols, lds, dst, ldd, src_off=0, dst_off=0):
@@ -64,14 +104,22 @@ def _mps_mpo_site(A, W, layout):
 
 
 def _scale_rows(A, d, mode=0):
-    f = torch.sqrt(d) if mode == 1 else d
-    A.mul_(f.to(A.dtype)[:, None])
+    A.mul_(_mode(d, mode).to(A.dtype)[:, None])
     return A
 
 
+def _mode(d, mode):
+    if mode == 1:
+        return torch.sqrt(d)
+    if mode == 2:
+        return torch.where(d > 0, 1 / d, torch.zeros_like(d))
+    if mode == 3:
+        return torch.where(d > 0, 1 / (d * d), torch.zeros_like(d))
+    return d
+
+
 def _scale_cols(A, d, mode=0):
-    f = torch.sqrt(d) if mode == 1 else d
-    A.mul_(f.to(A.dtype)[None, :])
+    A.mul_(_mode(d, mode).to(A.dtype)[None, :])
     return A
 
 
@@ -108,6 +156,9 @@ PATCH = {
     "svd": _svd,
     "qr": _qr,
     "truncation_rank": _trunc,
+    "gemm": _gemm,
+    "svd_rows": _svd_rows,
+    "gather_rows": _gather,
     "copy2d": _copy2d,
     "mps_mpo_site": _mps_mpo_site,
     "scale_rows": _scale_rows,

@@ -1,0 +1,121 @@
+"""Sweep engine and its Jacobi stage on the GPU, against the oracle and the
+reference's fixtures.  Fidelity-error bounds: 1e-10 for FP64 storage, 1e-6
+for FP32 storage (the tolerance of FP32-class paths)."""
+import numpy as np
+import pytest
+import torch
+
+import api_cases as K
+import tn_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rnd(rng, shape, dt):
+    a = rng.standard_normal(shape)
+    if np.iscomplexobj(np.zeros(0, dt)):
+        a = a + 1j * rng.standard_normal(shape)
+    return a.astype(dt)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64, np.complex64, np.complex128])
+@pytest.mark.parametrize("shape", [(2, 2), (3, 40), (40, 3), (33, 65), (96, 200), (260, 120), (512, 768)])
+def test_svd_rows(gpu, dt, shape):
+    from tncontract_gb300 import _ops
+    if np.dtype(dt).itemsize * (2 if np.iscomplexobj(np.zeros(0, dt)) else 1) >= 16 and max(shape) > 512:
+        pytest.skip("FP64 complex rows above 512 use the accumulating SVD")
+    if np.dtype(dt) == np.float64 and max(shape) > 512:
+        pytest.skip("FP64 rows above 512 use the accumulating SVD")
+    rng = np.random.default_rng(11)
+    A = rnd(rng, shape, dt)
+    W, S, order, info = _ops.svd_rows(torch.from_numpy(A).cuda())
+    assert int(info[0].item()) == 0
+    s = S.cpu().numpy()
+    s_ref = np.linalg.svd(A.astype(np.complex128), compute_uv=False)
+    tol = 2e-5 if np.dtype(dt) in (np.float32, np.complex64) else 1e-12
+    assert np.max(np.abs(s - s_ref)) < 10 * tol * np.sqrt(max(shape)) * s_ref[0]
+    Wh = W.cpu().numpy()[order.cpu().numpy()]
+    G = Wh @ np.conj(Wh).T
+    off = G - np.diag(np.diag(G))
+    assert np.linalg.norm(off) < 10 * tol * np.sqrt(max(shape)) * s_ref[0] ** 2 * np.sqrt(min(shape))
+
+
+def _run_engine(tn_engine, sites, mpo, chi, precision, cplx=True):
+    dt = tn_engine.compute_dtype(precision, cplx)
+    bal, ln = tn_engine.balance(sites)
+    S = tn_engine.to_sites(bal, dt)
+    Mo = tn_engine.to_sites(mpo, dt)
+    st = tn_engine.SweepStats()
+    out = tn_engine.apply_compress(S, Mo, chi, stats=st, log_norm_in=ln)
+    torch.cuda.synchronize()
+    return [o.cpu().numpy().astype(np.complex128) for o in out], st
+
+
+@pytest.mark.parametrize("precision,fid_tol", [("fp64", 1e-10), ("fp32", 1e-6)])
+def test_engine_config2_small(gpu, precision, fid_tol):
+    from tncontract_gb300 import engine as E
+    g, m = K.load("config2_small")
+    N, chi = 12, 16
+    sites = O.random_mps(0, N, 2, chi, np.complex128, normalise=True)
+    mpo = O.tfim_mpo(N)
+    got, st = _run_engine(E, sites, mpo, chi, precision)
+    assert [1] + [a.shape[2] for a in got] == m["c2s_m_bonds"]
+    ref = O.apply_compress_sweep(sites, mpo, chi)
+    assert 1 - O.fidelity(ref, got) < fid_tol
+    assert abs(O.mps_norm(got) - float(np.real(g["c2s_norm_m"]))) < fid_tol ** 0.5 * 10
+    for s, s_ref in zip(O.bond_spectra(got), K.unpack(g, "c2s_m_spectra")):
+        assert K.close(s, s_ref, 1e-8 if precision == "fp64" else 1e-4)
+
+
+@pytest.mark.parametrize("precision,fid_tol", [("fp64", 1e-10), ("fp32", 1e-6)])
+def test_engine_config2_chi128(gpu, precision, fid_tol):
+    """The benchmark unit at chi=128, N=64 (config 2) against the oracle."""
+    from tncontract_gb300 import engine as E
+    g, m = K.load("config2_chi128")
+    N, chi = 64, 128
+    sites = O.random_mps(0, N, 2, chi, np.complex128, normalise=True)
+    mpo = O.tfim_mpo(N)
+    got, st = _run_engine(E, sites, mpo, chi, precision)
+    assert [1] + [a.shape[2] for a in got] == m["c2_m_bonds"]
+    ref = O.apply_compress_sweep(sites, mpo, chi)
+    err = 1 - O.fidelity(ref, got)
+    assert err < fid_tol, err
+    phi = O.contract_mps_mpo(sites, mpo)
+    assert abs(O.fidelity(phi, got) - float(np.real(g["c2_fid_m_phi"]))) < 10 * fid_tol
+
+
+def test_engine_real_config1(gpu):
+    """Real float64 input (config 1 sizes) through the engine in FP64."""
+    from tncontract_gb300 import engine as E
+    sites = O.random_mps(0, 32, 2, 32, np.float64)
+    lc = O.left_canonical_form_mps(sites)
+    mpo = [np.eye(2).reshape(2, 2, 1, 1) for _ in range(32)]  # identity MPO
+    got, _ = _run_engine(E, lc, mpo, 16, "fp64", cplx=False)
+    ref = O.svd_compress_method(lc, 16)
+    assert 1 - O.fidelity(ref, got) < 1e-10
+
+
+def test_engine_batched(gpu):
+    from tncontract_gb300 import engine as E
+    N, chi = 16, 24
+    mpo = O.tfim_mpo(N)
+    batch_np = [O.random_mps(s, N, 2, chi, np.complex128, normalise=True) for s in range(4)]
+    dt = E.compute_dtype("fp32", True)
+    bal = [E.balance(b) for b in batch_np]
+    batch = [E.to_sites(b, dt) for b, _ in bal]
+    Mo = E.to_sites(mpo, dt)
+    outs = E.apply_compress_batch(batch, Mo, chi, log_norms=[ln for _, ln in bal])
+    torch.cuda.synchronize()
+    for b, out in zip(batch_np, outs):
+        got = [o.cpu().numpy().astype(np.complex128) for o in out]
+        ref = O.apply_compress_sweep(b, mpo, chi)
+        assert 1 - O.fidelity(ref, got) < 1e-6
+
+
+def test_engine_inner_product(gpu):
+    from tncontract_gb300 import engine as E
+    a = O.random_mps(5, 10, 3, 7, np.complex128)
+    b = O.random_mps(6, 10, 3, 7, np.complex128)
+    da = E.to_sites(a, torch.complex128)
+    db = E.to_sites(b, torch.complex128)
+    assert abs(E.inner_product(da, db) - O.inner_product(a, b)) < 1e-10 * abs(O.inner_product(a, b))

@@ -51,6 +51,9 @@ SIGNATURES = {
     "tnc_svd": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, C.c_size_t, _vp, _vp],
     "tnc_truncation_rank": [_int, _i64, _vp, _i64, _dbl, _int, _vp, _vp, _vp],
     "tnc_svd_noalloc": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, _vp],
+    "tnc_svd_rows_workspace_size": [_int, _i64, _i64, _psz],
+    "tnc_svd_rows": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _vp, C.c_size_t, _vp, _vp],
+    "tnc_gather_rows": [_int, _vp, _i64, _vp, _vp, _i64, _vp, _int, _vp, _vp],
 }
 
 RESTYPES = {"tnc_status_string": C.c_char_p, "tnc_kernel_launches": C.c_ulonglong}

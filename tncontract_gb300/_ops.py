@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import threading
 
 import numpy as np
 import torch
@@ -421,14 +422,99 @@ def qr(M, check=True):
     return Q, R
 
 
-def truncation_rank(S, chi, threshold, relative):
-    """(k, discarded weight) for descending singular values S (synchronises)."""
-    buf = torch.empty(2, dtype=torch.float64, device=device())
+def truncation_rank(S, chi, threshold, relative, with_smax=False, kdev_out=None):
+    """(k, discarded weight[, s_max]) for descending singular values S, read
+    back with one synchronising copy.  ``kdev_out`` (list) receives the device
+    int64 holding k."""
+    buf = torch.empty(3, dtype=torch.float64, device=device())
     kbuf = buf[0:1].view(torch.int64)
     _call("tnc_truncation_rank", code(S.dtype), S.numel(), _p(S), int(chi or 0), float(threshold),
           int(bool(relative)), _p(kbuf), C.c_void_p(buf.data_ptr() + 8), _stream())
+    if with_smax and S.numel():
+        _call("tnc_cast", code(S.dtype), L.F64, 1, _p(S), C.c_void_p(buf.data_ptr() + 16), _stream())
+    if kdev_out is not None:
+        kdev_out.append(kbuf)
     h = buf.cpu()
-    return int(h[0:1].view(torch.int64).item()), float(h[1].item())
+    k, disc = int(h[0:1].view(torch.int64).item()), float(h[1].item())
+    if with_smax:
+        return k, disc, (float(h[2].item()) if S.numel() else 0.0)
+    return k, disc
+
+
+_TUNE = {}            # (dtype, m, n) -> half-block height chosen by the autotuner
+_TUNE_LOCK = threading.Lock()
+TUNE_CANDIDATES = (4, 8, 16)
+
+
+def _svd_rows_call(M, W, S, order, info, h, max_sweeps, tol):
+    m, n = M.shape
+    sz = C.c_size_t()
+    _call("tnc_svd_rows_workspace_size", code(M.dtype), m, n, C.byref(sz))
+    ws = workspace(sz.value)
+    mm, nn = max(m, n), min(m, n)
+    _call("tnc_svd_rows", code(M.dtype), m, n, _p(M), _p(W), _p(S), _p(order), int(max_sweeps), float(tol),
+          int(h), _p(ws), sz.value, _p(info), _stream(),
+          flops=(6.0 * mm * nn * nn + 20.0 * nn ** 3) * (4 if is_complex(M.dtype) else 1))
+
+
+def tune_svd_rows(M, max_sweeps=0, tol=0.0):
+    """Autotuner: time each half-block height once on this shape (device
+    synchronised, CUDA events) and remember the fastest."""
+    m, n = M.shape
+    key = (M.dtype, m, n)
+    with _TUNE_LOCK:
+        if key in _TUNE:
+            return _TUNE[key]
+        nr, Lr = min(m, n), max(m, n)
+        W = empty((nr, Lr), M.dtype)
+        S = empty((nr,), real_dtype(M.dtype))
+        order = torch.empty(nr, dtype=torch.int64, device=device())
+        info = torch.empty(4, dtype=torch.int32, device=device())
+        best, best_ms = 8, None
+        global PROFILE
+        saved, PROFILE = PROFILE, None
+        try:
+            for h in TUNE_CANDIDATES:
+                torch.cuda.synchronize()
+                s = torch.cuda.Event(enable_timing=True)
+                e = torch.cuda.Event(enable_timing=True)
+                s.record()
+                _svd_rows_call(M, W, S, order, info, h, max_sweeps, tol)
+                e.record()
+                torch.cuda.synchronize()
+                ms = s.elapsed_time(e)
+                if best_ms is None or ms < best_ms:
+                    best, best_ms = h, ms
+        finally:
+            PROFILE = saved
+        _TUNE[key] = best
+        return best
+
+
+def svd_rows(M, max_sweeps=0, tol=0.0, block_rows=None):
+    """Jacobi stage of the sweep SVD (``tnc_svd_rows``): returns (W, S,
+    order, info) with W = orthogonalised rows of M (wide) or M^H (tall).
+    ``block_rows`` None = the autotuned half-block height for this shape."""
+    M = M.contiguous()
+    m, n = M.shape
+    nr, Lr = min(m, n), max(m, n)
+    if block_rows is None:
+        block_rows = _TUNE.get((M.dtype, m, n)) or tune_svd_rows(M, max_sweeps, tol)
+    W = empty((nr, Lr), M.dtype)
+    S = empty((nr,), real_dtype(M.dtype))
+    order = torch.empty(nr, dtype=torch.int64, device=device())
+    info = torch.empty(4, dtype=torch.int32, device=device())
+    _svd_rows_call(M, W, S, order, info, block_rows, max_sweeps, tol)
+    return W, S, order, info
+
+
+def gather_rows(W, order, kdev, kmax, S=None, mode=0):
+    """Rows order[:k] of W (mode 0: k x L) or conj(W[order[:k]])^T / S (mode 1: L x k)."""
+    Lr = W.shape[1]
+    out = empty((kmax, Lr) if mode == 0 else (Lr, kmax), W.dtype)
+    _call("tnc_gather_rows", code(W.dtype), _p(W), Lr, _p(order), _p(kdev), int(kmax),
+          _p(S) if S is not None else C.c_void_p(0), int(mode), _p(out), _stream())
+    return out
 
 
 def prod(shape):

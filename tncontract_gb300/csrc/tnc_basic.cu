@@ -275,6 +275,8 @@ __global__ void scale_rc_kernel(int64_t rows, int64_t cols, const typename trait
     int64_t i = e / cols, j = e - i * cols;
     typename traits<T>::real f = d[ROWS ? i : j];
     if (mode == 1) f = sqrt(f);
+    else if (mode == 2) f = (f > 0) ? 1 / f : 0;
+    else if (mode == 3) f = (f > 0) ? 1 / (f * f) : 0;
     A[i * lda + j] = A[i * lda + j] * f;
   }
 }

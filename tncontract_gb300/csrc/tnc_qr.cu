@@ -135,6 +135,194 @@ __global__ void qr_extract_r(const T* __restrict__ Bt, int64_t m, int64_t n, int
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident panel variant (columns of up to 32*E rows).
+//
+// Each warp keeps its column in registers (element i at lane i%32, slot i/32);
+// a CTA of kPanel warps owns kPanel consecutive columns (a panel).  Inside a
+// panel, reflector c is made by its owner warp, written to shared memory and
+// applied by the panel's later columns after a CTA barrier -- no global
+// round trip.  Each reflector is also published to global memory with a
+// flag; warps of later panels wait on the flag (bounded) and apply it from
+// registers loaded in one burst.  The critical path is the in-panel chain,
+// one CTA barrier per column.
+constexpr int kPanel = 8;
+
+template <typename T>
+__device__ __forceinline__ T shfl_T(T v, int src) {
+  if constexpr (traits<T>::is_complex) {
+    v.re = __shfl_sync(0xffffffffu, v.re, src);
+    v.im = __shfl_sync(0xffffffffu, v.im, src);
+    return v;
+  } else {
+    return __shfl_sync(0xffffffffu, v, src);
+  }
+}
+
+// value at row i of a register-resident column, broadcast to the warp
+template <typename T, int E>
+__device__ __forceinline__ T reg_get(const T (&x)[E], int64_t i) {
+  const int64_t slot = i >> 5;
+  T a = zero_<T>();
+#pragma unroll
+  for (int u = 0; u < E; ++u)
+    if (u == slot) a = x[u];
+  return shfl_T(a, (int)(i & 31));
+}
+
+// larfg on the register column: entries > c scaled to v, entry c = beta
+template <typename T, int E>
+__device__ __forceinline__ T make_reflector_reg(T (&x)[E], int64_t c, int64_t m) {
+  typedef typename traits<T>::real R;
+  const int lane = threadIdx.x & 31;
+  R xn = 0;
+#pragma unroll
+  for (int u = 0; u < E; ++u) {
+    const int64_t i = lane + 32 * u;
+    if (i > c && i < m) xn += abs2_(x[u]);
+  }
+  xn = warp_sum(xn);
+  const T alpha = reg_get(x, c);
+  T tau = zero_<T>();
+  if (!(xn == R(0) && imag_(alpha) == R(0))) {
+    const R beta = -copysign(sqrt(abs2_(alpha) + xn), real_(alpha));
+    const T betaT = from_real<T>(beta);
+    tau = div_(betaT - alpha, betaT);
+    const T scal = div_(one_<T>(), alpha - betaT);
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+      const int64_t i = lane + 32 * u;
+      if (i > c && i < m) x[u] = scal * x[u];
+      else if (i == c) x[u] = betaT;
+    }
+  }
+  return tau;
+}
+
+// x <- H_c^H x with v held in registers vv (v_c = 1 implied)
+template <typename T, int E>
+__device__ __forceinline__ void apply_reg(T (&x)[E], const T (&vv)[E], T tau, int64_t c, int64_t m) {
+  const int lane = threadIdx.x & 31;
+  T w = zero_<T>();
+#pragma unroll
+  for (int u = 0; u < E; ++u) {
+    const int64_t i = lane + 32 * u;
+    if (i == c) w += x[u];
+    else if (i > c && i < m) fma_(w, conj_(vv[u]), x[u]);
+  }
+  w = warp_sum(w);
+  const T f = conj_(tau) * w;
+#pragma unroll
+  for (int u = 0; u < E; ++u) {
+    const int64_t i = lane + 32 * u;
+    if (i == c) x[u] = x[u] - f;
+    else if (i > c && i < m) x[u] = x[u] - f * vv[u];
+  }
+}
+
+template <typename T, int E>
+__global__ void __launch_bounds__(kPanel * 32)
+qr_panel_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) {
+  __shared__ T sv[32 * E];
+  __shared__ T stau;
+  const int64_t k = m < n ? m : n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t p0 = (int64_t)blockIdx.x * kPanel;  // first column of the panel
+  const int64_t j = p0 + warp;                      // my column
+  const bool has = j < n;
+  T x[E];
+  T vv[E];
+  if (has) {
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+      const int64_t i = lane + 32 * u;
+      x[u] = (i < m) ? Bt[j * m + i] : zero_<T>();
+    }
+  }
+  // reflectors of earlier panels, as they are published
+  const int64_t cend = p0 < k ? p0 : k;
+  if (has) {
+    for (int64_t c = 0; c < cend; ++c) {
+      if (!warp_wait_flag(&flags[c], sw)) break;
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        const int64_t i = lane + 32 * u;
+        vv[u] = (i > c && i < m) ? ldcg(Bt + c * m + i) : zero_<T>();
+      }
+      apply_reg(x, vv, ldcg(tau + c), c, m);
+    }
+  }
+  __syncthreads();
+  if (ld_volatile(&sw->err)) return;  // uniform: every warp sees the same error word after the barrier
+  // this panel's reflectors
+  for (int w = 0; w < kPanel; ++w) {
+    const int64_t c = p0 + w;
+    if (c >= k) break;  // uniform over the CTA
+    if (warp == w) {
+      const T t = make_reflector_reg(x, c, m);
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        const int64_t i = lane + 32 * u;
+        if (i < m) {
+          sv[i] = x[u];
+          if (i >= c) stcg(Bt + c * m + i, x[u]);
+        }
+      }
+      if (lane == 0) {
+        stau = t;
+        stcg(tau + c, t);
+      }
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) atomicExch(&flags[c], 1);
+    }
+    __syncthreads();
+    if (has && warp > w) {
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        const int64_t i = lane + 32 * u;
+        vv[u] = (i > c && i < m) ? sv[i] : zero_<T>();
+      }
+      apply_reg(x, vv, stau, c, m);
+    }
+    __syncthreads();
+  }
+  if (has) {
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+      const int64_t i = lane + 32 * u;
+      if (i < m) Bt[j * m + i] = x[u];
+    }
+  }
+}
+
+// Qt[j] = H_{min(j,k-1)} ... H_0 e_j with the column in registers
+template <typename T, int E>
+__global__ void __launch_bounds__(kPanel * 32)
+qr_form_q_reg_kernel(const T* __restrict__ Bt, int64_t m, int64_t k, const T* __restrict__ tau, T* __restrict__ Qt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * kPanel;
+  for (int64_t j = (int64_t)blockIdx.x * kPanel + (threadIdx.x >> 5); j < k; j += nwarps) {
+    T x[E], vv[E];
+#pragma unroll
+    for (int u = 0; u < E; ++u) x[u] = (lane + 32 * u == j) ? one_<T>() : zero_<T>();
+    for (int64_t c = j; c >= 0; --c) {
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        const int64_t i = lane + 32 * u;
+        vv[u] = (i > c && i < m) ? Bt[c * m + i] : zero_<T>();
+      }
+      // H_c (not conjugated): x -= tau (v^H x) v
+      apply_reg(x, vv, conj_(tau[c]), c, m);
+    }
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+      const int64_t i = lane + 32 * u;
+      if (i < m) Qt[j * m + i] = x[u];
+    }
+  }
+}
+
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct QrLayout {
@@ -181,20 +369,49 @@ static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, vo
   if (cudaMemsetAsync(flags, 0, (size_t)k * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(info, 0, sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
-  const int threads = kQrWarps * 32;
-  int cap = coop_capacity((const void*)qr_factor_kernel<T>, threads, 0);
-  if (cap <= 0) return TNC_ERR_CUDA;
-  int64_t want = (n + kQrWarps - 1) / kQrWarps;
-  int grid = (int)(want < cap ? want : cap);
   int64_t mm = m, nn = n;
   void* args[] = {(void*)&Bt, (void*)&mm, (void*)&nn, (void*)&tau, (void*)&flags, (void*)&sw};
-  if (cudaLaunchCooperativeKernel((const void*)qr_factor_kernel<T>, dim3(grid), dim3(threads), args, 0, st) !=
-      cudaSuccess)
-    return TNC_ERR_CUDA;
+  // register-resident panels when the column fits (E slots of 32 rows)
+  const void* panel_fn = nullptr;
+  void (*formq_fn)(const T*, int64_t, int64_t, const T*, T*) = nullptr;
+  const int64_t slots = (m + 31) / 32;
+  const int64_t maxE = sizeof(T) >= 16 ? 16 : 48;
+  if (slots <= 8) { panel_fn = (const void*)qr_panel_kernel<T, 8>; formq_fn = qr_form_q_reg_kernel<T, 8>; }
+  else if (slots <= 16) { panel_fn = (const void*)qr_panel_kernel<T, 16>; formq_fn = qr_form_q_reg_kernel<T, 16>; }
+  else if constexpr (sizeof(T) < 16) {
+    if (slots <= 32 && maxE >= 32) { panel_fn = (const void*)qr_panel_kernel<T, 32>; formq_fn = qr_form_q_reg_kernel<T, 32>; }
+    else if (slots <= 48 && maxE >= 48) { panel_fn = (const void*)qr_panel_kernel<T, 48>; formq_fn = qr_form_q_reg_kernel<T, 48>; }
+  }
+  bool used_panel = false;
+  if (panel_fn != nullptr) {
+    const int64_t want = (n + kPanel - 1) / kPanel;
+    const int cap = coop_capacity(panel_fn, kPanel * 32, 0);
+    if (cap > 0 && want <= cap) {
+      if (cudaLaunchCooperativeKernel(panel_fn, dim3((unsigned)want), dim3(kPanel * 32), args, 0, st) != cudaSuccess)
+        return TNC_ERR_CUDA;
+      used_panel = true;
+    }
+  }
+  if (!used_panel) {
+    const int threads = kQrWarps * 32;
+    int cap = coop_capacity((const void*)qr_factor_kernel<T>, threads, 0);
+    if (cap <= 0) return TNC_ERR_CUDA;
+    int64_t want = (n + kQrWarps - 1) / kQrWarps;
+    int grid = (int)(want < cap ? want : cap);
+    if (cudaLaunchCooperativeKernel((const void*)qr_factor_kernel<T>, dim3(grid), dim3(threads), args, 0, st) !=
+        cudaSuccess)
+      return TNC_ERR_CUDA;
+  }
   copy_sync_error<<<1, 1, 0, st>>>(sw, info);
-  int64_t gq = (k + kQrWarps - 1) / kQrWarps;
-  if (gq > 152 * 16) gq = 152 * 16;
-  qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
+  if (formq_fn != nullptr) {
+    int64_t gq = (k + kPanel - 1) / kPanel;
+    formq_fn<<<(unsigned)gq, kPanel * 32, 0, st>>>(Bt, m, k, tau, Qt);
+  } else {
+    const int threads = kQrWarps * 32;
+    int64_t gq = (k + kQrWarps - 1) / kQrWarps;
+    if (gq > 152 * 16) gq = 152 * 16;
+    qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
+  }
   qr_extract_r<T><<<grid1d(k * n, 256), 256, 0, st>>>(Bt, m, n, k, R);
   if (launch_status(4)) return TNC_ERR_CUDA;  // factor, error copy, form Q, extract R
   // Q = Qt^T

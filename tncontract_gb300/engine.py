@@ -1,0 +1,256 @@
+"""Sweep engine: MPO-MPS apply + SVD compression on device-resident site
+arrays, batched over independent instances.
+
+This is the fast path behind the drop-in API.  It computes exactly what
+``contract_mps_mpo`` followed by ``MatrixProductState.svd_compress``
+(tncontract/onedim/onedim_core.py:1691-1708, 463-484) compute -- a QR left
+sweep, normalisation, a truncating SVD right sweep with the reference's rank
+rule (s/s_max > threshold, then at most chi, onedim_core.py:332-339) and the
+norm restored -- but on sites kept in one fixed layout (phys, left, right)
+so that no label bookkeeping or relayout runs per site, and with a precision
+option:
+
+* ``precision="fp64"``: complex128 / float64 storage and arithmetic;
+* ``precision="fp32"``: complex64 / float32 storage and arithmetic (the FP32
+  pipe of GB300 is 64x its FP64 pipe).  Fidelity error against the FP64
+  result is reported by the benchmark and checked by the tests.
+
+The truncating SVD of each site uses the block one-sided Jacobi of
+``tnc_svd_rows`` (rotations not accumulated) and recovers the second factor
+with one GEMM.  ``apply_compress_batch`` runs several instances at once, one
+CUDA stream and one host thread each (the native calls release the GIL), so
+the per-site latency chains of different instances overlap on the GPU.
+"""
+from __future__ import annotations
+
+import threading
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import _ops
+
+_DT = {"fp32": (torch.complex64, torch.float32), "fp64": (torch.complex128, torch.float64)}
+
+
+def compute_dtype(precision, is_complex):
+    return _DT[precision][0 if is_complex else 1]
+
+
+def to_sites(arrays, dtype):
+    """Host or device arrays (phys, left, right) -> contiguous device tensors of ``dtype``."""
+    return [_ops.cast(_ops.to_device(a), dtype) for a in arrays]
+
+
+def balance(arrays):
+    """Rescale every site to unit Frobenius norm (in the arrays' own
+    precision) and return (arrays, log_norm) with
+    state = exp(log_norm) * product of the rescaled sites.  A normalised
+    random MPS keeps a factor ~1e-86 (N=64, chi=256) in one site, below the
+    FP32 range; balanced sites keep every entry O(1)."""
+    out, log_norm = [], 0.0
+    for a in arrays:
+        if isinstance(a, torch.Tensor):
+            n = float(torch.linalg.vector_norm(a.reshape(-1).to(torch.complex128)).item()) if a.device.type == "cpu" \
+                else _ops.nrm2(a)
+            out.append(a / n if n > 0 else a)
+        else:
+            n = float(np.linalg.norm(a))
+            out.append(a / n if n > 0 else a)
+        log_norm += float(np.log(n)) if n > 0 else 0.0
+    return out, log_norm
+
+
+class SweepStats:
+    def __init__(self):
+        self.bonds = []
+        self.discarded = []      # per right-sweep bond, sum of discarded s^2 (normalised state)
+        self.jacobi_sweeps = []
+        self.norm = 1.0
+        self.log_norm = 0.0      # natural log of the output state's norm factor
+
+
+def apply_mpo(sites, mpo):
+    """contract_mps_mpo in (phys, left, right) layout: fused bond a*D + b."""
+    out = []
+    for A, W in zip(sites, mpo):
+        out.append(_ops.mps_mpo_site(A, _ops.cast(W, A.dtype) if W.dtype != A.dtype else W, layout=1))
+    return out
+
+
+def qr_left_sweep(P):
+    """QR branch of left_canonise (onedim_core.py:267-294), in place on P.
+    R is divided by its norm before it is absorbed (the gauge freedom makes
+    this exact); returns log of the state norm (sum of the removed log-norms
+    plus the last site's)."""
+    N = len(P)
+    log_norm = 0.0
+    for i in range(N - 1):
+        d, l, r = P[i].shape
+        Q, R = _ops.qr(P[i].reshape(d * l, r))
+        k = Q.shape[1]
+        P[i] = Q.reshape(d, l, k)
+        rn = _ops.nrm2(R)
+        if rn > 0:
+            log_norm += float(np.log(rn))
+        d2, l2, r2 = P[i + 1].shape
+        nxt = _ops.empty((d2, k, r2), P[i].dtype)
+        _ops.gemm(L.OP_N, L.OP_N, k, r2, r, R, r, P[i + 1], r2, nxt, r2,
+                  alpha=(1.0 / rn if rn > 0 else 1.0), batch=d2, sA=0, sB=r * r2, sC=k * r2)
+        P[i + 1] = nxt
+    last = _ops.nrm2(P[-1])
+    if last == 0.0:
+        raise ValueError("zero state in the QR sweep")
+    P[-1] = _ops.scale(P[-1], 1.0 / last)
+    return log_norm + float(np.log(last))
+
+
+def svd_right_sweep(P, chi, threshold, stats=None):
+    """Truncating SVD branch of right_canonise (reverse, left_canonise,
+    reverse; onedim_core.py:296-378) with normalise=False, in place on P."""
+    N = len(P)
+    norm_acc = 1.0
+    for i in range(N - 1, 0, -1):
+        d, l, r = P[i].shape
+        M = _ops.permute(P[i], (0, 2, 1)).reshape(d * r, l)  # rows (phys, right), cols left
+        m, n = M.shape
+        W, S, order, info = _ops.svd_rows(M)
+        kdev = []
+        k, disc, smax = _ops.truncation_rank(S, chi or 0, threshold, relative=True, with_smax=True,
+                                             kdev_out=kdev)
+        st = int(info[0].item())
+        if st != L.OK:
+            if st == L.ERR_NONFINITE:
+                raise ValueError("array must not contain infs or NaNs")
+            raise _ops.LinAlgError("SVD did not converge (status %d)" % st)
+        if smax == 0.0:
+            raise ValueError("zero state in the SVD sweep")
+        kd = kdev[0]
+        if m <= n:  # W rows = S V^H
+            SV = _ops.gather_rows(W, order, kd, k, mode=0)              # k x l
+            U = _ops.empty((m, k), M.dtype)
+            _ops.gemm(L.OP_N, L.OP_C, m, k, n, M, n, SV, n, U, k)       # M (S V^H)^H
+            _ops.scale_cols(U, S[:k].contiguous(), 3)                    # / S^2
+        else:       # W rows = S U^H
+            U = _ops.gather_rows(W, order, kd, k, S=S, mode=1)         # m x k
+            SV = _ops.empty((k, n), M.dtype)
+            _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)       # U^H M
+        P[i] = _ops.permute(U.reshape(d, r, k), (0, 2, 1))             # (phys, k, right)
+        dp, lp, rp = P[i - 1].shape                                      # rp == l
+        nxt = _ops.empty((dp, lp, k), M.dtype)
+        _ops.gemm(L.OP_N, L.OP_T, dp * lp, k, rp, P[i - 1], rp, SV, n, nxt, k, alpha=1.0 / smax)
+        P[i - 1] = nxt
+        norm_acc *= smax
+        if stats is not None:
+            stats.bonds.append(k)
+            stats.discarded.append(disc / (smax * smax))
+            stats.jacobi_sweeps.append(info)
+    P[0] = _ops.scale(P[0], norm_acc)
+    return norm_acc
+
+
+_FOLD_LIMIT = {torch.complex64: 60.0, torch.float32: 60.0}  # |log| folded into FP32 sites
+
+
+def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0):
+    """One unit: contract_mps_mpo then svd_compress(chi, threshold,
+    normalise=False).  ``sites`` / ``mpo`` are device tensors in (phys,
+    left, right) / (physout, physin, left, right) layout, all of the compute
+    dtype; the input state is exp(log_norm_in) times the product of
+    ``sites``.  Returns the compressed sites (phys, left, right) carrying the
+    state's norm in the first site, as svd_compress does; when that factor is
+    outside the storage range (FP32: |log| > 60) it is left out of the sites
+    and only reported in ``stats.log_norm``."""
+    P = apply_mpo(sites, mpo)
+    log_norm = qr_left_sweep(P) + log_norm_in
+    norm_acc = svd_right_sweep(P, chi, threshold, stats)
+    total = log_norm + (float(np.log(norm_acc)) if norm_acc > 0 else 0.0)
+    # svd_right_sweep already folded norm_acc into P[0]
+    lim = _FOLD_LIMIT.get(P[0].dtype, 600.0)
+    if abs(log_norm) <= lim:
+        P[0] = _ops.scale(P[0], float(np.exp(log_norm)))
+        folded = True
+    else:
+        folded = False
+    if stats is not None:
+        stats.norm = float(np.exp(total)) if abs(total) < 700 else float("inf")
+        stats.log_norm = total
+        stats.norm_folded = folded
+    return P
+
+
+def apply_compress_batch(batch, mpo, chi, threshold=1e-15, streams=None, stats=None, log_norms=None):
+    """``apply_compress`` for several independent instances at once: instance
+    b runs on its own CUDA stream from its own host thread.  ``batch`` is a
+    list of site lists (``log_norms[b]``: their log norm factors, see
+    ``balance``); returns the list of results (same order)."""
+    B = len(batch)
+    if streams is None:
+        streams = [torch.cuda.Stream() for _ in range(B)]
+    out = [None] * B
+    errs = [None] * B
+    dev = torch.cuda.current_device()
+    cur = torch.cuda.current_stream()
+
+    def run(b):
+        try:
+            torch.cuda.set_device(dev)
+            streams[b].wait_stream(cur)
+            with torch.cuda.stream(streams[b]):
+                out[b] = apply_compress(batch[b], mpo, chi, threshold,
+                                        stats[b] if stats is not None else None,
+                                        log_norms[b] if log_norms is not None else 0.0)
+        except BaseException as e:  # surfaced below
+            errs[b] = e
+
+    threads = [threading.Thread(target=run, args=(b,)) for b in range(B)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for e in errs:
+        if e is not None:
+            raise e
+    for s in streams:
+        cur.wait_stream(s)
+    return out
+
+
+def inner_product(bra, ket, conj_bra=True):
+    """<bra|ket> of two (phys, left, right) site lists on the device, by the
+    left-to-right environment sweep of ladder_contract (onedim_core.py:1587-1607).
+    Returns a Python complex."""
+    dt = torch.promote_types(bra[0].dtype, ket[0].dtype)
+    C = None
+    for a, b in zip(bra, ket):
+        a = _ops.cast(a, dt)
+        b = _ops.cast(b, dt)
+        if conj_bra:
+            a = _ops.conj(a)
+        d, la, ra = a.shape
+        _, lb, rb = b.shape
+        if C is None:
+            # boundary legs have dimension 1
+            Cn = _ops.empty((ra, rb), dt)
+            _ops.gemm(L.OP_T, L.OP_N, ra, rb, d, a.reshape(d, ra), ra, b.reshape(d, rb), rb, Cn, rb)
+            C = Cn
+            continue
+        # T[p][la? ...]: T = C^T-contract: T_p = C (la x lb) ; step 1: X_p = a_p^T C  (ra x lb)
+        X = _ops.empty((d, ra, lb), dt)
+        _ops.gemm(L.OP_T, L.OP_N, ra, lb, la, a, ra, C, lb, X, lb, batch=d, sA=la * ra, sB=0, sC=ra * lb)
+        # C' = sum_p X_p b_p  (ra x rb): one GEMM with K = d * lb
+        Cn = _ops.empty((ra, rb), dt)
+        Xp = _ops.permute(X, (1, 0, 2)).reshape(ra, d * lb)
+        _ops.gemm(L.OP_N, L.OP_N, ra, rb, d * lb, Xp, d * lb, b.reshape(d * lb, rb), rb, Cn, rb)
+        C = Cn
+    v = C.reshape(-1)[0].item()
+    return complex(v)
+
+
+def fidelity(a, b):
+    """|<a|b>|^2 / (<a|a><b|b>) on the device."""
+    ab = inner_product(a, b)
+    aa = inner_product(a, a).real
+    bb = inner_product(b, b).real
+    return abs(ab) ** 2 / (aa * bb)
