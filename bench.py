@@ -87,9 +87,11 @@ def run_micro(args):
     elif op == "qr":
         A = mat(*dims)
         fn = lambda: _ops.qr(A, check=False)
-    elif op == "gemm":
+    elif op in ("gemm", "gemmtc", "gemmsimt"):
         A, B = mat(dims[0], dims[2]), mat(dims[2], dims[1])
-        fn = lambda: _ops.matmul(A, B)
+        Cm = torch.empty((dims[0], dims[1]), dtype=A.dtype, device="cuda")
+        tc = {"gemm": None, "gemmtc": True, "gemmsimt": False}[op]
+        fn = lambda: _ops.gemm(0, 0, dims[0], dims[1], dims[2], A, dims[2], B, dims[1], Cm, dims[1], tc=tc)
     elif op.startswith("svdrows"):
         A = mat(*dims)
         h = int(op[7:]) if len(op) > 7 else None
@@ -109,7 +111,8 @@ def run_micro(args):
     torch.cuda.synchronize()
     summ = _ops.profile_summary(_ops.PROFILE)
     _ops.PROFILE = None
-    name = {"svd": "tnc_svd", "qr": "tnc_qr", "gemm": "tnc_gemm"}.get(op, "tnc_svd_rows")
+    name = {"svd": "tnc_svd", "qr": "tnc_qr", "gemmsimt": "tnc_gemm", "gemmtc": "tnc_gemm_tc",
+            "gemm": "tnc_gemm_tc" if "tnc_gemm_tc" in summ else "tnc_gemm"}.get(op, "tnc_svd_rows")
     n, ms, fl = summ[name]
     extra = {}
     if infos:

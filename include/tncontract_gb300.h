@@ -130,6 +130,23 @@ int tnc_gemm(int dtype, int opA, int opB, int64_t m, int64_t n, int64_t k,
              void *C, int64_t ldc, int64_t strideC, int64_t batch,
              void *stream);
 
+/* tnc_gemm on the tcgen05 tensor cores for F32 / C64: TF32 split products
+ * (hi*hi + hi*lo + lo*hi, FP32 accumulation in tensor memory) give
+ * FP32-class accuracy; operands are split into planar K-major TF32 planes in
+ * the workspace and streamed by TMA.  Same operands and ops as tnc_gemm;
+ * batch <= 65535.  The product np.tensordot performs (tensor.py:735) for
+ * single-precision tensors, and the absorption products of the sweep. */
+int tnc_gemm_tc_workspace_size(int dtype, int64_t m, int64_t n, int64_t k,
+                               int64_t batch, size_t *bytes);
+int tnc_gemm_tc(int dtype, int opA, int opB, int64_t m, int64_t n, int64_t k,
+                const double *alpha, const void *A, int64_t lda,
+                int64_t strideA, const void *B, int64_t ldb, int64_t strideB,
+                const double *beta, void *C, int64_t ldc, int64_t strideC,
+                int64_t batch, void *work, size_t work_bytes, void *stream);
+/* Reads and clears the tensor-core GEMM's device error flag (1 = a bounded
+ * wait gave up; synchronous). */
+int tnc_gemm_tc_error(void);
+
 /* One MPO-MPS site product with the reference's fused bond layout
  * (contract_mps_mpo, onedim_core.py:1702-1704: contract over phys/physin
  * then consolidate_indices, fused bond = a*D + b):
@@ -193,8 +210,8 @@ int tnc_svd_noalloc(int dtype, int64_t m, int64_t n, const void *A,
  * buffer), S = row norms sorted descending (real type of dtype) and order
  * (int64: order[i] = row of W holding the i-th singular triplet).  For a wide
  * A, rows order[:k] of W are S_k V_k^H and U_k = A (S_k V_k^H)^H S_k^-2; for
- * a tall A they are S_k U_k^H and S_k V_k^H = U_k^H A.  block_rows (2, 4, 8
- * or 16; anything else selects 8) is the half-block height, chosen per shape
+ * a tall A they are S_k U_k^H and S_k V_k^H = U_k^H A.  block_rows (2, 4 or
+ * 8; anything else selects 8) is the half-block height, chosen per shape
  * by the caller's autotuner.  max(m,n) <= 1024
  * (512 for F64/C128).  info as for tnc_svd. */
 int tnc_svd_rows_workspace_size(int dtype, int64_t m, int64_t n, size_t *bytes);

@@ -220,3 +220,40 @@ def test_mps_mpo_site(gpu, dt):
     assert relerr(out1, ref) < tol(dt)
     out0 = host(_ops.mps_mpo_site(dev(A), dev(W), 0))
     assert relerr(out0, np.transpose(ref, (1, 0, 2))) < tol(dt)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex64])
+def test_gemm_tensor_core(gpu, dt):
+    """tcgen05 TF32-split GEMM against NumPy (FP64) at FP32-class tolerance,
+    all op combinations, ragged sizes, batch and alpha/beta."""
+    from tncontract_gb300 import _lib, _ops
+    rng = np.random.default_rng(12)
+    opf = {0: lambda x: x, 1: lambda x: x.T, 2: lambda x: np.conj(x).T, 3: np.conj}
+    for (m, n, k) in [(128, 128, 32), (200, 136, 100), (512, 256, 768), (65, 300, 64)]:
+        for opA in range(4):
+            for opB in range(4):
+                A = rnd(rng, (k, m) if opA in (1, 2) else (m, k), dt)
+                B = rnd(rng, (n, k) if opB in (1, 2) else (k, n), dt)
+                Cm = torch.empty((m, n), dtype=torch.from_numpy(np.zeros(0, dt)).dtype, device="cuda")
+                _ops.gemm(opA, opB, m, n, k, dev(A), A.shape[1], dev(B), B.shape[1], Cm, n, tc=True)
+                ref = opf[opA](A.astype(np.complex128)) @ opf[opB](B.astype(np.complex128))
+                if not np.iscomplexobj(A):
+                    ref = ref.real
+                # TF32 split products accumulated in FP32 in tensor memory:
+                # ~1e-5 relative at K=768 complex (3072 real terms per output)
+                assert relerr(host(Cm), ref) < 3e-5, (m, n, k, opA, opB, relerr(host(Cm), ref))
+    assert _lib.lib().tnc_gemm_tc_error() == 0
+    # batched with alpha, beta
+    b, m, n, k = 3, 130, 70, 96
+    A = rnd(rng, (b, m, k), dt)
+    B = rnd(rng, (b, k, n), dt)
+    C0 = rnd(rng, (b, m, n), dt)
+    Cd = dev(C0)
+    al, be = (0.5 - 1j, 2j) if np.iscomplexobj(A) else (0.5, -2.0)
+    _ops.gemm(0, 0, m, n, k, dev(A), k, dev(B), n, Cd, n, alpha=al, beta=be, batch=b,
+              sA=m * k, sB=k * n, sC=m * n, tc=True)
+    ref = al * np.einsum("bmk,bkn->bmn", A.astype(np.complex128), B) + be * C0
+    if not np.iscomplexobj(A):
+        ref = ref.real
+    assert relerr(host(Cd), ref) < 3e-5
+    assert _lib.lib().tnc_gemm_tc_error() == 0

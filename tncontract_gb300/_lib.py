@@ -54,6 +54,10 @@ SIGNATURES = {
     "tnc_svd_rows_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_svd_rows": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _vp, C.c_size_t, _vp, _vp],
     "tnc_gather_rows": [_int, _vp, _i64, _vp, _vp, _i64, _vp, _int, _vp, _vp],
+    "tnc_gemm_tc_workspace_size": [_int, _i64, _i64, _i64, _i64, _psz],
+    "tnc_gemm_tc": [_int, _int, _int, _i64, _i64, _i64, _pdbl, _vp, _i64, _i64, _vp, _i64, _i64, _pdbl,
+                    _vp, _i64, _i64, _i64, _vp, C.c_size_t, _vp],
+    "tnc_gemm_tc_error": [],
 }
 
 RESTYPES = {"tnc_status_string": C.c_char_p, "tnc_kernel_launches": C.c_ulonglong}

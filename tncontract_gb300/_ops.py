@@ -294,11 +294,38 @@ def dot_device(x, y, conj_x=False):
 # ------------------------------------------------------------------ contraction
 
 
+# FP32-class GEMMs at least this large (m*n*k*batch) run on the tcgen05
+# tensor-core kernel (TF32 split products); smaller ones and FP64 use the
+# CUDA-core kernel.
+USE_TC = True
+TC_MIN_WORK = 1 << 21
+_TC_WS = {}
+
+
+def _tc_workspace(nbytes):
+    key = (torch.cuda.current_device(), torch.cuda.current_stream().cuda_stream)
+    buf = _TC_WS.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 1 << 20), dtype=torch.uint8, device=device())
+        _TC_WS[key] = buf
+    return buf
+
+
 def gemm(opA, opB, m, n, k, A, lda, B, ldb, Cm, ldc, alpha=1.0, beta=0.0,
-         batch=1, sA=0, sB=0, sC=0):
-    _call("tnc_gemm", code(Cm.dtype), opA, opB, m, n, k, _pair(alpha), _p(A), lda, sA,
-          _p(B), ldb, sB, _pair(beta), _p(Cm), ldc, sC, batch, _stream(),
-          flops=2.0 * m * n * k * batch * (4 if is_complex(Cm.dtype) else 1))
+         batch=1, sA=0, sB=0, sC=0, tc=None):
+    flops = 2.0 * m * n * k * batch * (4 if is_complex(Cm.dtype) else 1)
+    dt = code(Cm.dtype)
+    use_tc = (USE_TC if tc is None else tc) and dt in (L.F32, L.C64) and min(m, n) >= 64 and k >= 32 \
+        and m * n * k * batch >= TC_MIN_WORK and batch <= 65535
+    if use_tc:
+        sz = C.c_size_t()
+        _call("tnc_gemm_tc_workspace_size", dt, m, n, k, batch, C.byref(sz))
+        ws = _tc_workspace(sz.value)
+        _call("tnc_gemm_tc", dt, opA, opB, m, n, k, _pair(alpha), _p(A), lda, sA,
+              _p(B), ldb, sB, _pair(beta), _p(Cm), ldc, sC, batch, _p(ws), sz.value, _stream(), flops=flops)
+        return Cm
+    _call("tnc_gemm", dt, opA, opB, m, n, k, _pair(alpha), _p(A), lda, sA,
+          _p(B), ldb, sB, _pair(beta), _p(Cm), ldc, sC, batch, _stream(), flops=flops)
     return Cm
 
 
@@ -443,7 +470,7 @@ def truncation_rank(S, chi, threshold, relative, with_smax=False, kdev_out=None)
 
 _TUNE = {}            # (dtype, m, n) -> half-block height chosen by the autotuner
 _TUNE_LOCK = threading.Lock()
-TUNE_CANDIDATES = (4, 8, 16)
+TUNE_CANDIDATES = (4, 8)
 
 
 def _svd_rows_call(M, W, S, order, info, h, max_sweeps, tol):

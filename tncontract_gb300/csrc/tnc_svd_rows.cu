@@ -150,7 +150,7 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
 }
 
 template <typename T, int MAXE>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(256)
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, unsigned* counters,
                     SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
@@ -385,7 +385,7 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
     // half-block height: 16 rows (fewest barriers) when the shared-memory half
     // block and the register row fit, else smaller
     int h = 8;
-    if (block_rows == 2 || block_rows == 4 || block_rows == 8 || block_rows == 16) h = block_rows;
+    if (block_rows == 2 || block_rows == 4 || block_rows == 8) h = block_rows;
     while (h > 2 && (size_t)h * L * sizeof(T) > kMaxHalfBlockBytes) h >>= 1;
     while (h > 2 && h / 2 >= nr) h >>= 1;
     const bool big = sizeof(T) >= 16;
