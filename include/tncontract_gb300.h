@@ -229,6 +229,34 @@ int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
                     const int64_t *k, int64_t kmax, const void *S, int mode,
                     void *dst, void *stream);
 
+/* ------------------------------------------------------------ learned rank
+ * Kernels of the rank predictor (a small MLP trained on singular spectra the
+ * plain method produces) and of the randomized-SVD sketch it sizes.  No
+ * counterpart in the reference; they size a randomized SVD that stands in
+ * for left_canonise's full SVD (onedim_core.py:317) when the predicted rank
+ * is small, with the full SVD as fallback.  FP32, row-major, batch-major. */
+/* out[b][o] = act(sum_i W[o][i] in[b][i] + bias[o]); act 0 identity, 1 relu, 2 sigmoid */
+int tnc_dense_forward(const float *W, const float *bias, const float *in,
+                      float *out, int batch, int nin, int nout, int act,
+                      void *stream);
+/* dW = g^T in, db = colsum(g); gin = (g W) masked by act_in > 0 when
+ * relu_mask (gin may be NULL) */
+int tnc_dense_backward(const float *W, const float *in, const float *act_in,
+                       const float *g, float *dW, float *db, float *gin,
+                       int batch, int nin, int nout, int relu_mask,
+                       void *stream);
+/* g = d(mean squared error)/dz for y = sigmoid(z) */
+int tnc_mse_sigmoid_grad(const float *y, const float *target, float *g,
+                         int batch, void *stream);
+/* one Adam step with bias correction (step >= 1) */
+int tnc_adam_step(float *params, const float *grads, float *m, float *v,
+                  int64_t n, double lr, double beta1, double beta2,
+                  double eps, int step, void *stream);
+/* i.i.d. standard normal entries (complex: re and im each N(0,1)),
+ * counter-based: entry i depends only on (seed, i) */
+int tnc_fill_gaussian(int dtype, int64_t n, uint64_t seed, void *out,
+                      void *stream);
+
 /* Truncation decision on descending singular values S (n, real type of
  * dtype): k = #{ s_i > t } capped at chi (chi <= 0: no cap), t = threshold
  * (relative = 0) or threshold * S[0] (relative = 1).  Writes k (device

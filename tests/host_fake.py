@@ -149,7 +149,50 @@ def _axpby(alpha, x, beta, y):
     return y
 
 
+def _fill_gaussian(shape, dtype, seed):
+    rng = np.random.default_rng(int(seed) & 0xFFFFFFFF)
+    a = rng.standard_normal(shape)
+    if dtype.is_complex:
+        a = a + 1j * rng.standard_normal(shape)
+    return torch.from_numpy(a).to(dtype)
+
+
+def _dense_forward(W, b, x, nin, nout, act):
+    y = x @ W.reshape(nout, nin).T + b
+    if act == 1:
+        y = torch.relu(y)
+    elif act == 2:
+        y = torch.sigmoid(y)
+    return y.contiguous()
+
+
+def _dense_backward(W, x, act_in, g, dW, db, gin, nin, nout, relu_mask):
+    g = g.reshape(-1, nout)
+    dW.copy_((g.T @ x).reshape(-1))
+    db.copy_(g.sum(0))
+    if gin is not None:
+        r = g @ W.reshape(nout, nin)
+        if relu_mask:
+            r = r * (act_in > 0)
+        gin.copy_(r)
+
+
+def _mse_sigmoid_grad(y, t):
+    return (2 * (y - t) * y * (1 - y) / y.shape[0]).contiguous()
+
+
+def _adam_step(p, g, m, v, lr, b1, b2, eps, step):
+    m.mul_(b1).add_((1 - b1) * g)
+    v.mul_(b2).add_((1 - b2) * g * g)
+    p.sub_(lr * (m / (1 - b1 ** step)) / (torch.sqrt(v / (1 - b2 ** step)) + eps))
+
+
 PATCH = {
+    "fill_gaussian": _fill_gaussian,
+    "dense_forward": _dense_forward,
+    "dense_backward": _dense_backward,
+    "mse_sigmoid_grad": _mse_sigmoid_grad,
+    "adam_step": _adam_step,
     "device": lambda: torch.device("cpu"),
     "permute": _permute,
     "tensordot": _tensordot,

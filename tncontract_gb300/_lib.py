@@ -58,6 +58,11 @@ SIGNATURES = {
     "tnc_gemm_tc": [_int, _int, _int, _i64, _i64, _i64, _pdbl, _vp, _i64, _i64, _vp, _i64, _i64, _pdbl,
                     _vp, _i64, _i64, _i64, _vp, C.c_size_t, _vp],
     "tnc_gemm_tc_error": [],
+    "tnc_dense_forward": [_vp, _vp, _vp, _vp, _int, _int, _int, _int, _vp],
+    "tnc_dense_backward": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _int, _int, _int, _int, _vp],
+    "tnc_mse_sigmoid_grad": [_vp, _vp, _vp, _int, _vp],
+    "tnc_adam_step": [_vp, _vp, _vp, _vp, _i64, _dbl, _dbl, _dbl, _dbl, _int, _vp],
+    "tnc_fill_gaussian": [_int, _i64, C.c_uint64, _vp, _vp],
 }
 
 RESTYPES = {"tnc_status_string": C.c_char_p, "tnc_kernel_launches": C.c_ulonglong}

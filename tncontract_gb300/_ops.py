@@ -535,6 +535,36 @@ def svd_rows(M, max_sweeps=0, tol=0.0, block_rows=None):
     return W, S, order, info
 
 
+def fill_gaussian(shape, dtype, seed):
+    out = empty(shape, dtype)
+    if out.numel():
+        _call("tnc_fill_gaussian", code(dtype), out.numel(), int(seed) & ((1 << 63) - 1), _p(out), _stream())
+    return out
+
+
+def dense_forward(W, b, x, nin, nout, act):
+    out = empty((x.shape[0], nout), torch.float32)
+    _call("tnc_dense_forward", _p(W), _p(b), _p(x), _p(out), x.shape[0], nin, nout, int(act), _stream())
+    return out
+
+
+def dense_backward(W, x, act_in, g, dW, db, gin, nin, nout, relu_mask):
+    _call("tnc_dense_backward", _p(W), _p(x), _p(act_in) if act_in is not None else C.c_void_p(0), _p(g),
+          _p(dW), _p(db), _p(gin) if gin is not None else C.c_void_p(0), g.shape[0], nin, nout,
+          int(relu_mask), _stream())
+
+
+def mse_sigmoid_grad(y, t):
+    g = empty((y.shape[0],), torch.float32)
+    _call("tnc_mse_sigmoid_grad", _p(y), _p(t.contiguous()), _p(g), y.shape[0], _stream())
+    return g
+
+
+def adam_step(p, g, m, v, lr, b1, b2, eps, step):
+    _call("tnc_adam_step", _p(p), _p(g), _p(m), _p(v), p.numel(), float(lr), float(b1), float(b2), float(eps),
+          int(step), _stream())
+
+
 def gather_rows(W, order, kdev, kmax, S=None, mode=0):
     """Rows order[:k] of W (mode 0: k x L) or conj(W[order[:k]])^T / S (mode 1: L x k)."""
     Lr = W.shape[1]

@@ -23,6 +23,7 @@ the per-site latency chains of different instances overlap on the GPU.
 """
 from __future__ import annotations
 
+import math
 import threading
 
 import numpy as np
@@ -106,36 +107,164 @@ def qr_left_sweep(P):
     return log_norm + float(np.log(last))
 
 
-def svd_right_sweep(P, chi, threshold, stats=None):
+def _rows_limit(dtype):
+    return 512 if dtype in (torch.complex128, torch.float64) else 1024
+
+
+def _check_info(info):
+    st = int(info[0].item())
+    if st != L.OK:
+        if st == L.ERR_NONFINITE:
+            raise ValueError("array must not contain infs or NaNs")
+        raise _ops.LinAlgError("SVD did not converge (status %d)" % st)
+
+
+def _factor_full(M):
+    """Full SVD of M (m x n) -> (S device, S host, factors(k) -> (U_k, SV_k)).
+    Rows up to the register limit use the non-accumulating block Jacobi;
+    longer rows use the accumulating SVD."""
+    m, n = M.shape
+    if max(m, n) <= _rows_limit(M.dtype):
+        W, S, order, info = _ops.svd_rows(M)
+        _check_info(info)
+
+        def factors(k, kdev):
+            if m <= n:  # W rows = S V^H
+                SV = _ops.gather_rows(W, order, kdev, k, mode=0)          # k x n
+                U = _ops.empty((m, k), M.dtype)
+                _ops.gemm(L.OP_N, L.OP_C, m, k, n, M, n, SV, n, U, k)     # M (S V^H)^H
+                _ops.scale_cols(U, S[:k].contiguous(), 3)                  # / S^2
+            else:       # W rows = S U^H
+                U = _ops.gather_rows(W, order, kdev, k, S=S, mode=1)      # m x k
+                SV = _ops.empty((k, n), M.dtype)
+                _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)     # U^H M
+            return U, SV
+        return S, factors
+    U, S, VH = _ops.svd(M)
+
+    def factors(k, kdev):
+        Uk = _ops.slice_last(U, k) if k < U.shape[1] else U
+        SV = VH[:k].contiguous().clone()
+        _ops.scale_rows(SV, S[:k].contiguous(), 0)
+        return Uk, SV
+    return S, factors
+
+
+def _factor_sketch(M, l, power_iters, seed):
+    """Randomized range finder (Halko, Martinsson & Tropp 2011, alg. 4.4):
+    Q = orth((M M^H)^q M Omega) with Omega n x l Gaussian, re-orthonormalised
+    after every product; then the SVD of B = Q^H M (l x n).  Returns
+    (S, factors, captured weight fraction residual) with factors mapping to
+    (U = Q U_B, S V^H)."""
+    m, n = M.shape
+    dt = M.dtype
+    Om = _ops.fill_gaussian((n, l), dt, seed)
+    Y = _ops.empty((m, l), dt)
+    _ops.gemm(L.OP_N, L.OP_N, m, l, n, M, n, Om, l, Y, l)
+    for _ in range(power_iters):
+        Q, _r = _ops.qr(Y)
+        Z = _ops.empty((n, l), dt)
+        _ops.gemm(L.OP_C, L.OP_N, n, l, m, M, n, Q, l, Z, l)     # M^H Q
+        Q2, _r = _ops.qr(Z)
+        _ops.gemm(L.OP_N, L.OP_N, m, l, n, M, n, Q2, l, Y, l)    # M Q2
+    Q, _r = _ops.qr(Y)                                            # m x l
+    B = _ops.empty((l, n), dt)
+    _ops.gemm(L.OP_C, L.OP_N, l, n, m, Q, l, M, n, B, n)          # Q^H M
+    # residual weight |M - Q Q^H M|_F^2, formed explicitly: the difference of
+    # |M|^2 and |B|^2 would sit below FP32 resolution at small tolerances
+    E = M.clone()
+    _ops.gemm(L.OP_N, L.OP_N, m, n, l, Q, l, B, n, E, n, alpha=-1.0, beta=1.0)
+    residual = _ops.nrm2(E) ** 2
+    S, fB = _factor_full(B)
+
+    def factors(k, kdev):
+        UB, SV = fB(k, kdev)                                       # l x k, k x n
+        U = _ops.empty((m, k), dt)
+        _ops.gemm(L.OP_N, L.OP_N, m, k, l, Q, l, UB, k, U, k)
+        return U, SV
+    return S, factors, residual
+
+
+class RankStats:
+    def __init__(self):
+        self.features = []   # per bond, the predictor's input
+        self.targets = []    # per bond, k / min(m, n) chosen by the rule (full SVD only)
+        self.sketched = 0
+        self.fallbacks = 0
+        self.full = 0
+        self.rows_factored = 0   # sum over bonds of (rows of the Jacobi problem)^2 * row length
+
+
+def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None, oversample=16,
+                    power_iters=2, rank_stats=None, seed=1234):
     """Truncating SVD branch of right_canonise (reverse, left_canonise,
-    reverse; onedim_core.py:296-378) with normalise=False, in place on P."""
+    reverse; onedim_core.py:296-378) with normalise=False, in place on P.
+
+    Rank rule: the reference's (s/s_max > threshold, then at most chi) when
+    ``dw_tol`` is None; otherwise the smallest rank whose discarded weight
+    sum_{j>=k} s_j^2 is at most dw_tol * sum_j s_j^2 (capped at chi).  With a
+    ``rank_model`` (and ``dw_tol``), each bond's rank is predicted from the
+    neighbouring spectrum and a randomized SVD of that size + ``oversample``
+    replaces the full SVD; when the sketch leaves more than dw_tol of the
+    weight uncaptured the full SVD runs instead (fallback)."""
+    from . import rank_model as RM
     N = len(P)
     norm_acc = 1.0
+    s_prev = None
     for i in range(N - 1, 0, -1):
         d, l, r = P[i].shape
         M = _ops.permute(P[i], (0, 2, 1)).reshape(d * r, l)  # rows (phys, right), cols left
         m, n = M.shape
-        W, S, order, info = _ops.svd_rows(M)
-        kdev = []
-        k, disc, smax = _ops.truncation_rank(S, chi or 0, threshold, relative=True, with_smax=True,
-                                             kdev_out=kdev)
-        st = int(info[0].item())
-        if st != L.OK:
-            if st == L.ERR_NONFINITE:
-                raise ValueError("array must not contain infs or NaNs")
-            raise _ops.LinAlgError("SVD did not converge (status %d)" % st)
+        kmax = min(m, n)
+        used_sketch = False
+        feats = None
+        if dw_tol is not None and rank_stats is not None or rank_model is not None:
+            feats = RM.spectrum_features((i - 1) / max(N - 2, 1), kmax, chi or kmax, dw_tol or 1e-16,
+                                         s_prev if s_prev is not None else np.ones(1))
+        if rank_model is not None and dw_tol is not None and s_prev is not None:
+            frac = float(rank_model.predict(feats)[0])
+            lsk = min(kmax, int(math.ceil(frac * kmax)) + oversample)
+            if lsk < 0.75 * kmax:
+                total = _ops.nrm2(M) ** 2
+                S, factors, residual = _factor_sketch(M, lsk, power_iters, seed + i)
+                s_host = S.cpu().numpy().astype(np.float64)
+                if residual <= dw_tol * total:
+                    used_sketch = True
+                    # rank by the same rule, the uncaptured weight counted as discarded
+                    k = RM.dw_rank(s_host, dw_tol, chi or 0, total=float((s_host ** 2).sum()) + residual)
+                    smax = float(s_host[0])
+                    disc = float((s_host[k:] ** 2).sum()) + residual
+                    kd = torch.tensor([k], dtype=torch.int64, device=M.device)
+                    if rank_stats is not None:
+                        rank_stats.sketched += 1
+                        rank_stats.rows_factored += lsk * lsk * max(lsk, n)
+                elif rank_stats is not None:
+                    rank_stats.fallbacks += 1
+        if not used_sketch:
+            S, factors = _factor_full(M)
+            if dw_tol is None:
+                kdev = []
+                k, disc, smax = _ops.truncation_rank(S, chi or 0, threshold, relative=True, with_smax=True,
+                                                     kdev_out=kdev)
+                kd = kdev[0]
+                s_host = None
+            else:
+                s_host = S.cpu().numpy().astype(np.float64)
+                k = RM.dw_rank(s_host, dw_tol, chi or 0)
+                smax = float(s_host[0])
+                disc = float((s_host[k:] ** 2).sum())
+                kd = torch.tensor([k], dtype=torch.int64, device=M.device)
+            if rank_stats is not None:
+                rank_stats.full += 1
+                rank_stats.rows_factored += kmax * kmax * max(m, n)
+                if feats is not None and s_prev is not None:
+                    rank_stats.features.append(feats)
+                    rank_stats.targets.append(k / kmax)
         if smax == 0.0:
             raise ValueError("zero state in the SVD sweep")
-        kd = kdev[0]
-        if m <= n:  # W rows = S V^H
-            SV = _ops.gather_rows(W, order, kd, k, mode=0)              # k x l
-            U = _ops.empty((m, k), M.dtype)
-            _ops.gemm(L.OP_N, L.OP_C, m, k, n, M, n, SV, n, U, k)       # M (S V^H)^H
-            _ops.scale_cols(U, S[:k].contiguous(), 3)                    # / S^2
-        else:       # W rows = S U^H
-            U = _ops.gather_rows(W, order, kd, k, S=S, mode=1)         # m x k
-            SV = _ops.empty((k, n), M.dtype)
-            _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)       # U^H M
+        if rank_stats is not None or rank_model is not None:
+            s_prev = s_host if s_host is not None else S.cpu().numpy().astype(np.float64)
+        U, SV = factors(k, kd)
         P[i] = _ops.permute(U.reshape(d, r, k), (0, 2, 1))             # (phys, k, right)
         dp, lp, rp = P[i - 1].shape                                      # rp == l
         nxt = _ops.empty((dp, lp, k), M.dtype)
@@ -145,7 +274,6 @@ def svd_right_sweep(P, chi, threshold, stats=None):
         if stats is not None:
             stats.bonds.append(k)
             stats.discarded.append(disc / (smax * smax))
-            stats.jacobi_sweeps.append(info)
     P[0] = _ops.scale(P[0], norm_acc)
     return norm_acc
 
@@ -153,7 +281,8 @@ def svd_right_sweep(P, chi, threshold, stats=None):
 _FOLD_LIMIT = {torch.complex64: 60.0, torch.float32: 60.0}  # |log| folded into FP32 sites
 
 
-def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0):
+def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0, dw_tol=None,
+                   rank_model=None, rank_stats=None, oversample=16, power_iters=2):
     """One unit: contract_mps_mpo then svd_compress(chi, threshold,
     normalise=False).  ``sites`` / ``mpo`` are device tensors in (phys,
     left, right) / (physout, physin, left, right) layout, all of the compute
@@ -161,10 +290,12 @@ def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0
     ``sites``.  Returns the compressed sites (phys, left, right) carrying the
     state's norm in the first site, as svd_compress does; when that factor is
     outside the storage range (FP32: |log| > 60) it is left out of the sites
-    and only reported in ``stats.log_norm``."""
+    and only reported in ``stats.log_norm``.  ``dw_tol``, ``rank_model``,
+    ``rank_stats``, ``oversample``, ``power_iters``: see svd_right_sweep."""
     P = apply_mpo(sites, mpo)
     log_norm = qr_left_sweep(P) + log_norm_in
-    norm_acc = svd_right_sweep(P, chi, threshold, stats)
+    norm_acc = svd_right_sweep(P, chi, threshold, stats, dw_tol=dw_tol, rank_model=rank_model,
+                               oversample=oversample, power_iters=power_iters, rank_stats=rank_stats)
     total = log_norm + (float(np.log(norm_acc)) if norm_acc > 0 else 0.0)
     # svd_right_sweep already folded norm_acc into P[0]
     lim = _FOLD_LIMIT.get(P[0].dtype, 600.0)
