@@ -172,11 +172,27 @@ int tnc_qr(int dtype, int64_t m, int64_t n, const void *A, int64_t lda,
            void *Q, void *R, void *work, size_t work_bytes, int *info,
            void *stream);
 
+/* R factor only of a dense row-major m x n matrix A (adjoint = 0; R is
+ * k x n) or of its conjugate transpose A^H (adjoint = 1; R is k x m),
+ * k = min(m, n); Q is not formed.  The sweep SVD preconditions its Jacobi
+ * stage with the R of M^H: the rotated rows of R are S U^H of M, so U comes
+ * out orthonormal whatever the spectrum, and the Jacobi converges in fewer
+ * sweeps on graded matrices.  No counterpart in the reference (whose
+ * tensor_svd calls LAPACK gesdd on M directly, tensor.py:915). */
+int tnc_qr_r_workspace_size(int dtype, int64_t m, int64_t n, int adjoint,
+                            size_t *bytes);
+int tnc_qr_r(int dtype, int64_t m, int64_t n, const void *A, int adjoint,
+             void *R, void *work, size_t work_bytes, int *info, void *stream);
+
 /* Thin SVD of a row-major m x n matrix A (lda): U is m x k, S has k real
  * values sorted descending (float for F32/C64, double for F64/C128), VH is
- * k x n, k = min(m, n).  One-sided (Hestenes) Jacobi with a round-robin
- * ordering, run by one persistent cooperative launch.  max_sweeps <= 0
- * selects 40; tol <= 0 selects sqrt(max(m,n)) * eps.  info (device, 4 ints):
+ * k x n, k = min(m, n).  QR-preconditioned one-sided (Hestenes) Jacobi:
+ * the k x k triangular factor of A^H (wide A) or A (tall A) is
+ * orthogonalised with a round-robin ordering by one persistent cooperative
+ * launch, rotations accumulated; U and VH follow with one GEMM against Q,
+ * both orthonormal however graded the spectrum.  max_sweeps <= 0 selects
+ * 40; tol <= 0 selects sqrt(k) * eps (4x that for FP32 storage).  info
+ * (device, 4 ints):
  * [0] status (TNC_OK / TNC_ERR_NOT_CONVERGED / TNC_ERR_NONFINITE /
  * TNC_ERR_TIMEOUT), [1] sweeps used, [2] rotations in the last sweep.
  * Replaces np.linalg.svd(full_matrices=False) in tensor_svd (tensor.py:915)

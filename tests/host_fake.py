@@ -38,6 +38,12 @@ def _qr(M):
     return torch.from_numpy(q), torch.from_numpy(r)
 
 
+def _qr_r(M, adjoint=False, check=True):
+    X = M.numpy()
+    X = np.conj(X).T if adjoint else X
+    return torch.from_numpy(np.ascontiguousarray(np.linalg.qr(X, mode="r")))
+
+
 def _trunc(S, chi, threshold, relative, with_smax=False, kdev_out=None):
     s = S.numpy()
     keep = s[:chi] if chi else s
@@ -198,6 +204,7 @@ PATCH = {
     "tensordot": _tensordot,
     "svd": _svd,
     "qr": _qr,
+    "qr_r": _qr_r,
     "truncation_rank": _trunc,
     "gemm": _gemm,
     "svd_rows": _svd_rows,

@@ -40,6 +40,40 @@ def test_svd_rows(gpu, dt, shape):
     assert np.linalg.norm(off) < 10 * tol * np.sqrt(max(shape)) * s_ref[0] ** 2 * np.sqrt(min(shape))
 
 
+@pytest.mark.parametrize("dt", [np.float32, np.complex64, np.float64, np.complex128])
+@pytest.mark.parametrize("shape", [(200, 300), (300, 200), (256, 256), (600, 300)])
+def test_factor_full_graded(gpu, dt, shape):
+    """The sweep factorisation on a graded matrix whose spectrum falls from 1
+    to 1e-40 (the boundary-MPS matrices of a PEPS norm network look like
+    this): converges, U orthonormal for every direction the rank rule keeps,
+    U (S V^H) = M up to the discarded weight, S against LAPACK.  FP64 with
+    600 rows takes the accumulating-SVD branch."""
+    from tncontract_gb300 import engine as E
+    rng = np.random.default_rng(21)
+    m, n = shape
+    k = min(m, n)
+    cplx = np.iscomplexobj(np.zeros(0, dt))
+    Ux = np.linalg.qr(rnd(rng, (m, k), np.complex128 if cplx else np.float64))[0]
+    Vx = np.linalg.qr(rnd(rng, (n, k), np.complex128 if cplx else np.float64))[0]
+    s_true = 10.0 ** (-40.0 * np.arange(k) / (k - 1))
+    M = ((Ux * s_true) @ np.conj(Vx).T).astype(dt)
+    single = np.dtype(dt) in (np.float32, np.complex64)
+    S, factors = E._factor_full(torch.from_numpy(M).cuda())
+    s_ref = np.linalg.svd(M.astype(np.complex128), compute_uv=False)
+    s = S.cpu().numpy().astype(np.float64)
+    tol = 2e-5 if single else 1e-12
+    assert np.max(np.abs(s - s_ref)) < 10 * tol * np.sqrt(max(shape)) * s_ref[0]
+    # the engine's rule: the reference's threshold, capped at the noise floor
+    kk = min(E.reference_rank(s, 0, 1e-14), E.noise_rank(s, torch.from_numpy(M).dtype))
+    assert kk >= int(np.count_nonzero(s_ref > (1e-5 if single else 1e-13) * s_ref[0]))
+    U, SV = factors(kk, torch.tensor([kk], dtype=torch.int64, device="cuda"))
+    U = U.cpu().numpy().astype(np.complex128)
+    SV = SV.cpu().numpy().astype(np.complex128)
+    assert np.linalg.norm(np.conj(U).T @ U - np.eye(kk)) < 100 * tol * np.sqrt(kk)
+    err = np.linalg.norm(U @ SV - M.astype(np.complex128)) / np.linalg.norm(M.astype(np.complex128))
+    assert err < 10 * tol * np.sqrt(max(shape))
+
+
 def _run_engine(tn_engine, sites, mpo, chi, precision, cplx=True):
     dt = tn_engine.compute_dtype(precision, cplx)
     bal, ln = tn_engine.balance(sites)

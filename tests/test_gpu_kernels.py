@@ -105,6 +105,26 @@ def test_qr(gpu, dt, shape):
     assert np.allclose(np.imag(np.diag(R)), 0, atol=t)
 
 
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (40, 13), (13, 40), (256, 512), (700, 300)])
+def test_qr_r_only(gpu, dt, shape):
+    """tnc_qr_r: R of A and of A^H equal the R of the full QR of the same
+    matrix (same reflectors, Q not formed)."""
+    from tncontract_gb300 import _ops
+    rng = np.random.default_rng(14)
+    A = rnd(rng, shape, dt)
+    for adjoint in (False, True):
+        X = np.ascontiguousarray(np.conj(A).T) if adjoint else A
+        R = host(_ops.qr_r(dev(A), adjoint=adjoint))
+        _, Rfull = _ops.qr(dev(X))
+        Rfull = host(Rfull)
+        assert R.shape == Rfull.shape == (min(shape), X.shape[1])
+        assert relerr(R, Rfull) < tol(dt)
+        # R^H R = X^H X
+        t = tol(dt) * max(shape)
+        assert relerr(np.conj(R).T @ R, np.conj(X).T @ X) < t
+
+
 def test_qr_rank_deficient(gpu):
     from tncontract_gb300 import _ops
     rng = np.random.default_rng(5)

@@ -39,3 +39,38 @@ def test_config2_small_host():
     import tncontract_gb300 as tn
     with cpu_ops():
         K.check_config2_small(tn)
+
+
+def test_engine_rank_rules():
+    """The engine's host-side rank rule equals the reference's (s/s_max >
+    threshold, then at most chi) and is capped at the storage noise floor."""
+    import numpy as np
+    import torch
+    from tncontract_gb300 import engine as E
+    s = np.array([1.0, 0.5, 1e-3, 1e-9, 1e-15, 0.0])
+    assert E.reference_rank(s, 0, 1e-14) == 4
+    assert E.reference_rank(s, 3, 1e-14) == 3
+    assert E.reference_rank(s, 0, 1e-3) == 2          # strictly greater than threshold * s_max
+    assert E.reference_rank(np.zeros(3), 0, 1e-14) == 0
+    assert E.noise_rank(s, torch.float64) == 5        # 1e-15 > 4 eps |s| ~ 1e-15
+    assert E.noise_rank(s, torch.float32) == 3        # FP32 floor ~ 5e-7
+    assert E.noise_rank(s, torch.complex64) == 3
+
+
+def test_boundary_mps_engine_host():
+    """engine.boundary_mps_contract (control flow, layouts, log-norm
+    bookkeeping) with the CPU stand-in, against the reference's PEPS norm
+    values: 4x4 D=2 chi=4 and 8x8 D=4 chi=16."""
+    import numpy as np
+    import tn_oracle as O
+    from tncontract_gb300 import engine as E
+    from tncontract_gb300 import workloads as W
+    g, m = K.load("peps")
+    with cpu_ops():
+        rows = O.random_peps(2, 4, 4, 2, 2)
+        val, log10, _ = E.boundary_mps_contract(W.double_layer_arrays(rows), 4, precision="fp64")
+        assert abs(val - float(g["p4_value"])) < 1e-10 * float(g["p4_value"])
+        rows = W.random_peps_arrays(2, 8, 8, 4, 2)
+        val, log10, _ = E.boundary_mps_contract(W.double_layer_arrays(rows), 16, precision="fp64")
+        assert abs(log10 - m["p8c16_log10"]) < 1e-10
+        assert np.isfinite(log10)

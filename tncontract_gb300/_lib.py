@@ -47,6 +47,8 @@ SIGNATURES = {
     "tnc_mps_mpo_site": [_int, _i64, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _int, _vp],
     "tnc_qr_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_qr": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, C.c_size_t, _vp, _vp],
+    "tnc_qr_r_workspace_size": [_int, _i64, _i64, _int, _psz],
+    "tnc_qr_r": [_int, _i64, _i64, _vp, _int, _vp, _vp, C.c_size_t, _vp, _vp],
     "tnc_svd_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_svd": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, C.c_size_t, _vp, _vp],
     "tnc_truncation_rank": [_int, _i64, _vp, _i64, _dbl, _int, _vp, _vp, _vp],

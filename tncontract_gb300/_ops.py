@@ -449,6 +449,29 @@ def qr(M, check=True):
     return Q, R
 
 
+def qr_r(M, adjoint=False, check=True):
+    """R factor of the QR of M (m x n; R is min(m, n) x n) or, with
+    ``adjoint``, of M^H (R is min(m, n) x m); Q is not formed."""
+    M = M.contiguous()
+    m, n = M.shape
+    k = min(m, n)
+    R = empty((k, m if adjoint else n), M.dtype)
+    if k == 0:
+        return R
+    sz = C.c_size_t()
+    _call("tnc_qr_r_workspace_size", code(M.dtype), m, n, int(bool(adjoint)), C.byref(sz))
+    ws = workspace(sz.value)
+    info = torch.empty(1, dtype=torch.int32, device=device())
+    mm, nn = max(m, n), min(m, n)
+    _call("tnc_qr_r", code(M.dtype), m, n, _p(M), int(bool(adjoint)), _p(R), _p(ws), sz.value, _p(info),
+          _stream(), flops=(2.0 * mm * nn * nn - 2.0 / 3.0 * nn ** 3) * (4 if is_complex(M.dtype) else 1))
+    if check:
+        st = int(info.item())
+        if st != L.OK:
+            raise L.NativeError("tnc_qr_r", st)
+    return R
+
+
 def truncation_rank(S, chi, threshold, relative, with_smax=False, kdev_out=None):
     """(k, discarded weight[, s_max]) for descending singular values S, read
     back with one synchronising copy.  ``kdev_out`` (list) receives the device

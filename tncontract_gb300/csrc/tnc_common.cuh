@@ -62,6 +62,15 @@ template <typename R> __host__ __device__ inline cplx<R> conj_(cplx<R> a) { retu
 __host__ __device__ inline float abs2_(float x) { return x * x; }
 __host__ __device__ inline double abs2_(double x) { return x * x; }
 template <typename R> __host__ __device__ inline R abs2_(cplx<R> a) { return a.re * a.re + a.im * a.im; }
+// |x| without squaring (x*x underflows for |x| below ~1e-19 in FP32)
+__device__ __forceinline__ float abs_(float x) { return fabsf(x); }
+__device__ __forceinline__ double abs_(double x) { return fabs(x); }
+__device__ __forceinline__ float abs_(cplx<float> a) { return hypotf(a.re, a.im); }
+__device__ __forceinline__ double abs_(cplx<double> a) { return hypot(a.re, a.im); }
+// x / h for real h (a division, so a denormal h does not overflow 1/h)
+__device__ __forceinline__ float div_real_(float x, float h) { return x / h; }
+__device__ __forceinline__ double div_real_(double x, double h) { return x / h; }
+template <typename R> __device__ __forceinline__ cplx<R> div_real_(cplx<R> x, R h) { return {x.re / h, x.im / h}; }
 
 __host__ __device__ inline float real_(float x) { return x; }
 __host__ __device__ inline double real_(double x) { return x; }
@@ -163,5 +172,14 @@ int gemm_launch(int opA, int opB, int64_t m, int64_t n, int64_t k, T alpha,
                 const T* A, int64_t lda, int64_t sA, const T* B, int64_t ldb,
                 int64_t sB, T beta, T* C, int64_t ldc, int64_t sC,
                 int64_t batch, cudaStream_t st);
+
+// Householder QR of X (fm x fn): X = A (adjoint = 0, A dense fm x fn) or
+// X = A^H (adjoint = 1, A dense fn x fm).  Writes R (min(fm,fn) x fn); with
+// want_qt also forms Q^T (min(fm,fn) x fm, row-major) inside the workspace
+// and returns its address in *qt.  Workspace: qr_qt_workspace(fm, fn, es).
+size_t qr_qt_workspace(int64_t fm, int64_t fn, size_t es);
+template <typename T>
+int qr_qt(int64_t fm, int64_t fn, const T* A, int adjoint, bool want_qt, T* R, void* work, size_t wb, int* info,
+          cudaStream_t st, T** qt);
 
 }  // namespace tnc

@@ -194,6 +194,28 @@ static __global__ void copy_sync_error(const SyncWords* sw, int* info) {
   if (e) info[0] = e;
 }
 
+// out[0] += sum |x|^2 over n elements (double accumulation, one atomic per
+// block; out zeroed by the caller).  The Jacobi kernels read it as the
+// squared Frobenius norm, which their rotations preserve.
+template <typename T>
+static __global__ void frob2_kernel(int64_t n, const T* __restrict__ x, double* out) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)abs2_(x[i]);
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) atomicAdd(out, acc);
+}
+
+// Squared row norm at or below which a row is rounding noise of a matrix with
+// squared Frobenius norm f2: (eps |W|_F)^2.  Such rows take part in no
+// rotation (their directions carry no information, and in FP32 their
+// products fall into the denormal range where they lose all precision).
+template <typename T>
+__device__ __forceinline__ typename traits<T>::real noise_floor2(const double* f2) {
+  return (typename traits<T>::real)(traits<T>::eps * traits<T>::eps * f2[0]);
+}
+
 // Largest co-resident grid for a cooperative launch of `kernel`.
 inline int coop_capacity(const void* kernel, int threads, size_t smem) {
   int dev = 0, sms = 0, per = 0, coop = 0;

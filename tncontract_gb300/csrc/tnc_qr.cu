@@ -342,30 +342,23 @@ static QrLayout qr_layout(int64_t m, int64_t n, size_t es) {
 }
 
 template <typename T>
-static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, void* work, size_t wb,
-                   int* info, cudaStream_t st) {
-  if (m <= 0 || n <= 0 || lda < n || !A || !Q || !R || !work || !info) return TNC_ERR_ARG;
-  QrLayout L = qr_layout(m, n, sizeof(T));
-  if (wb < L.total) return TNC_ERR_WORKSPACE;
+static int dtype_of() {
+  return sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128);
+}
+
+// Householder factorisation of the m x n matrix X whose transpose is already
+// in Bt (n x m, dense).  R (k x n) is always extracted; the rows of Q^T
+// (k x m, in the workspace at L.qt) are formed when want_qt or Q is set, and
+// Q = (Q^T)^T (m x k) is written when Q is not null.
+template <typename T>
+static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const QrLayout& L, char* w, int* info,
+                        cudaStream_t st) {
   const int64_t k = m < n ? m : n;
-  char* w = (char*)work;
   T* Bt = (T*)(w + L.bt);
   T* tau = (T*)(w + L.tau);
   int* flags = (int*)(w + L.flags);
   SyncWords* sw = (SyncWords*)(w + L.sync);
   T* Qt = (T*)(w + L.qt);
-  // Bt = A^T (A may have lda > n: transpose through the GEMM-free permute
-  // path only handles dense input, so copy row blocks with a strided GEMM-less
-  // 2-D transpose)
-  if (lda == n) {
-    int64_t shp[2] = {m, n};
-    int perm[2] = {1, 0};
-    int s = tnc_permute(sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128),
-                        A, Bt, 2, shp, perm, 0, st);
-    if (s) return s;
-  } else {
-    return TNC_ERR_ARG;
-  }
   if (cudaMemsetAsync(flags, 0, (size_t)k * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(info, 0, sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
@@ -393,6 +386,7 @@ static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, vo
     }
   }
   if (!used_panel) {
+    formq_fn = nullptr;
     const int threads = kQrWarps * 32;
     int cap = coop_capacity((const void*)qr_factor_kernel<T>, threads, 0);
     if (cap <= 0) return TNC_ERR_CUDA;
@@ -403,23 +397,95 @@ static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, vo
       return TNC_ERR_CUDA;
   }
   copy_sync_error<<<1, 1, 0, st>>>(sw, info);
-  if (formq_fn != nullptr) {
-    int64_t gq = (k + kPanel - 1) / kPanel;
-    formq_fn<<<(unsigned)gq, kPanel * 32, 0, st>>>(Bt, m, k, tau, Qt);
-  } else {
-    const int threads = kQrWarps * 32;
-    int64_t gq = (k + kQrWarps - 1) / kQrWarps;
-    if (gq > 152 * 16) gq = 152 * 16;
-    qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
+  int launches = 3;  // factor, error copy, extract R
+  if (Q != nullptr || want_qt) {
+    if (formq_fn != nullptr) {
+      int64_t gq = (k + kPanel - 1) / kPanel;
+      formq_fn<<<(unsigned)gq, kPanel * 32, 0, st>>>(Bt, m, k, tau, Qt);
+    } else {
+      const int threads = kQrWarps * 32;
+      int64_t gq = (k + kQrWarps - 1) / kQrWarps;
+      if (gq > 152 * 16) gq = 152 * 16;
+      qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
+    }
+    ++launches;
   }
   qr_extract_r<T><<<grid1d(k * n, 256), 256, 0, st>>>(Bt, m, n, k, R);
-  if (launch_status(4)) return TNC_ERR_CUDA;  // factor, error copy, form Q, extract R
+  if (launch_status(launches)) return TNC_ERR_CUDA;
+  if (Q == nullptr) return TNC_OK;
   // Q = Qt^T
   int64_t shp[2] = {k, m};
   int perm[2] = {1, 0};
-  return tnc_permute(sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128),
-                     Qt, Q, 2, shp, perm, 0, st);
+  return tnc_permute(dtype_of<T>(), Qt, Q, 2, shp, perm, 0, st);
 }
+
+template <typename T>
+static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, void* work, size_t wb,
+                   int* info, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || lda < n || !A || !Q || !R || !work || !info) return TNC_ERR_ARG;
+  if (lda != n) return TNC_ERR_ARG;
+  QrLayout L = qr_layout(m, n, sizeof(T));
+  if (wb < L.total) return TNC_ERR_WORKSPACE;
+  char* w = (char*)work;
+  // Bt = A^T
+  int64_t shp[2] = {m, n};
+  int perm[2] = {1, 0};
+  if (int s = tnc_permute(dtype_of<T>(), A, (T*)(w + L.bt), 2, shp, perm, 0, st)) return s;
+  return qr_factor_bt<T>(m, n, Q, false, R, L, w, info, st);
+}
+
+// R factor only, of A (m x n) or, with adjoint, of A^H (n x m).  For A^H the
+// transposed copy the factorisation works on is conj(A) itself, so no
+// transpose runs.
+template <typename T>
+static int qr_r_impl(int64_t m, int64_t n, const T* A, int adjoint, T* R, void* work, size_t wb, int* info,
+                     cudaStream_t st) {
+  if (m <= 0 || n <= 0 || !A || !R || !work || !info) return TNC_ERR_ARG;
+  const int64_t fm = adjoint ? n : m, fn = adjoint ? m : n;  // the factorised matrix is fm x fn
+  QrLayout L = qr_layout(fm, fn, sizeof(T));
+  if (wb < L.total) return TNC_ERR_WORKSPACE;
+  char* w = (char*)work;
+  if (adjoint) {
+    int64_t shp[2] = {m, n};
+    int perm[2] = {0, 1};
+    if (int s = tnc_permute(dtype_of<T>(), A, (T*)(w + L.bt), 2, shp, perm, traits<T>::is_complex ? 1 : 0, st))
+      return s;
+  } else {
+    int64_t shp[2] = {m, n};
+    int perm[2] = {1, 0};
+    if (int s = tnc_permute(dtype_of<T>(), A, (T*)(w + L.bt), 2, shp, perm, 0, st)) return s;
+  }
+  return qr_factor_bt<T>(fm, fn, (T*)nullptr, false, R, L, w, info, st);
+}
+
+}  // namespace tnc
+
+namespace tnc {
+
+size_t qr_qt_workspace(int64_t fm, int64_t fn, size_t es) { return qr_layout(fm, fn, es).total; }
+
+template <typename T>
+int qr_qt(int64_t fm, int64_t fn, const T* A, int adjoint, bool want_qt, T* R, void* work, size_t wb, int* info,
+          cudaStream_t st, T** qt) {
+  if (fm <= 0 || fn <= 0 || !A || !R || !work || !info) return TNC_ERR_ARG;
+  QrLayout L = qr_layout(fm, fn, sizeof(T));
+  if (wb < L.total) return TNC_ERR_WORKSPACE;
+  char* w = (char*)work;
+  // Bt = X^T: for X = A^H that is conj(A) as stored (A is fn x fm)
+  int64_t shp[2] = {adjoint ? fn : fm, adjoint ? fm : fn};
+  int perm_id[2] = {0, 1}, perm_t[2] = {1, 0};
+  if (int s = tnc_permute(dtype_of<T>(), A, (T*)(w + L.bt), 2, shp, adjoint ? perm_id : perm_t,
+                          (adjoint && traits<T>::is_complex) ? 1 : 0, st))
+    return s;
+  if (qt) *qt = (T*)(w + L.qt);
+  return qr_factor_bt<T>(fm, fn, (T*)nullptr, want_qt, R, L, w, info, st);
+}
+
+template int qr_qt<float>(int64_t, int64_t, const float*, int, bool, float*, void*, size_t, int*, cudaStream_t, float**);
+template int qr_qt<double>(int64_t, int64_t, const double*, int, bool, double*, void*, size_t, int*, cudaStream_t,
+                           double**);
+template int qr_qt<c64>(int64_t, int64_t, const c64*, int, bool, c64*, void*, size_t, int*, cudaStream_t, c64**);
+template int qr_qt<c128>(int64_t, int64_t, const c128*, int, bool, c128*, void*, size_t, int*, cudaStream_t, c128**);
 
 }  // namespace tnc
 
@@ -436,5 +502,19 @@ extern "C" int tnc_qr(int dtype, int64_t m, int64_t n, const void* A, int64_t ld
                       size_t work_bytes, int* info, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   TNC_DISPATCH(dtype, T, return qr_impl<T>(m, n, (const T*)A, lda, (T*)Q, (T*)R, work, work_bytes, info, st));
+  return TNC_ERR_ARG;
+}
+
+extern "C" int tnc_qr_r_workspace_size(int dtype, int64_t m, int64_t n, int adjoint, size_t* bytes) {
+  int es = elem_size(dtype);
+  if (!es || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
+  *bytes = adjoint ? qr_layout(n, m, es).total : qr_layout(m, n, es).total;
+  return TNC_OK;
+}
+
+extern "C" int tnc_qr_r(int dtype, int64_t m, int64_t n, const void* A, int adjoint, void* R, void* work,
+                        size_t work_bytes, int* info, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  TNC_DISPATCH(dtype, T, return qr_r_impl<T>(m, n, (const T*)A, adjoint, (T*)R, work, work_bytes, info, st));
   return TNC_ERR_ARG;
 }

@@ -1,12 +1,12 @@
 // Thin SVD (np.linalg.svd(full_matrices=False) in tensor_svd,
 // tncontract/tensor.py:915, and its scipy gesvd retry, :916-929).
 //
-// One-sided (Hestenes) Jacobi on the ROWS of a working matrix W (nr x L,
-// nr <= L): pairs of rows are rotated until all rows are mutually orthogonal
-// to within tol.  The rotations are accumulated into J (nr x nr, rows), so
-//   W0 = J^H W,  W = D Y  (D = row norms, Y orthonormal rows)
-// is an SVD of the original W0 = (J^H) D Y.  For a wide A (m <= n) W0 = A;
-// for a tall A, W0 = A^H and the roles of U and V swap.
+// One-sided (Hestenes) Jacobi on the ROWS of a working matrix W (nr x nr):
+// pairs of rows are rotated until all rows are mutually orthogonal to within
+// tol.  The rotations are accumulated into J (nr x nr, rows), so
+//   W0 = J^H W,  W = D Y  (D = row norms, Y orthonormal rows).
+// W0 is the triangular factor of a QR preconditioning step (svd_impl below
+// says how U and VH of A follow from Y, D, J and Q).
 //
 // Parallel ordering: round-robin tournament over the rows (nr-1 rounds of
 // nr/2 disjoint pairs per sweep), one warp per pair, the whole iteration in
@@ -35,8 +35,8 @@ __device__ __forceinline__ void pair_indices(int64_t np, int64_t r, int64_t i, i
 
 template <typename T>
 __global__ void __launch_bounds__(kSvdWarps * 32)
-jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, unsigned* counters, SyncWords* sw,
-              int* info) {
+jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, const double* frob2,
+              unsigned* counters, SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
   const int64_t gw = (int64_t)blockIdx.x * kSvdWarps + (threadIdx.x >> 5);
@@ -44,6 +44,7 @@ jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, uns
   const int64_t np = nr + (nr & 1);
   const int64_t npairs = np / 2;
   const R rtol = (R)tol;
+  const R noise2 = noise_floor2<T>(frob2);
   int sweep = 0;
   bool converged = false;
   unsigned last_rot = 0;
@@ -59,15 +60,16 @@ jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, uns
         R a, b;
         T g;
         warp_pair_dots(x, y, L, a, b, g);
-        const R h = sqrt(abs2_(g));
-        if (!(h > rtol * sqrt(a) * sqrt(b))) continue;  // also skips NaN / zero rows
+        const R h = abs_(g);
+        // also skips NaN rows, rows at the rounding-noise floor and rows whose squared norm underflowed
+        if (!(a > noise2 && b > noise2 && a > 0 && b > 0 && h > rtol * sqrt(a) * sqrt(b))) continue;
         const R tau = (b - a) / (2 * h);
         R t;
         if (fabs(tau) > (R)1e15) t = (R)0.5 / tau;
         else t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
         const R c = R(1) / sqrt(R(1) + t * t);
         const R s = c * t;
-        const T e = g * (R(1) / h);
+        const T e = div_real_(g, h);
         const T se = s * e, sec = s * conj_(e);
         warp_pair_rotate(x, y, L, c, se, sec);
         if (J != nullptr) warp_pair_rotate(J + p * nr, J + q * nr, nr, c, se, sec);
@@ -81,7 +83,7 @@ jacobi_kernel(T* W, T* J, int64_t nr, int64_t L, int max_sweeps, double tol, uns
     if (last_rot == 0) { converged = true; ++sweep; break; }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    info[0] = converged ? TNC_OK : TNC_ERR_NOT_CONVERGED;
+    if (!converged) info[0] = TNC_ERR_NOT_CONVERGED;  // else keep the QR's status (OK or its timeout)
     info[1] = sweep;
     info[2] = (int)last_rot;
   }
@@ -157,16 +159,20 @@ __global__ void svd_output_kernel(const T* W, const T* J, const typename traits<
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct SvdLayout {
-  size_t w, j, d, pos, counters, sync, total;
+  size_t qr, w, j, d, frob2, pos, counters, sync, total;
 };
 static const int kMaxSweepsCap = 100;
+// [QR workspace of X (L x nr): its transposed copy, reused for the small
+//  output factor once R is out; tau; flags; Q^T] [W = R, nr x nr] [J] ...
 static SvdLayout svd_layout(int64_t m, int64_t n, size_t es, size_t rs) {
   int64_t nr = m < n ? m : n, L = m < n ? n : m;
   SvdLayout Ly;
   size_t off = 0;
-  Ly.w = off; off = align256(off + (size_t)nr * L * es);
+  Ly.qr = off; off = align256(off + qr_qt_workspace(L, nr, es));
+  Ly.w = off; off = align256(off + (size_t)nr * nr * es);
   Ly.j = off; off = align256(off + (size_t)nr * nr * es);
   Ly.d = off; off = align256(off + (size_t)nr * rs);
+  Ly.frob2 = off; off = align256(off + sizeof(double));
   Ly.pos = off; off = align256(off + (size_t)nr * sizeof(int64_t));
   Ly.counters = off; off = align256(off + kMaxSweepsCap * sizeof(unsigned));
   Ly.sync = off; off = align256(off + sizeof(SyncWords));
@@ -180,6 +186,17 @@ template <> int dtype_of<double>() { return TNC_F64; }
 template <> int dtype_of<c64>() { return TNC_C64; }
 template <> int dtype_of<c128>() { return TNC_C128; }
 
+// QR-preconditioned one-sided Jacobi (Drmac & Veselic 2008).  X is the
+// matrix whose columns the Jacobi would orthogonalise (X = A^H for a wide A,
+// X = A for a tall one; L x nr).  X = Q R, and the rows of R (nr x nr) are
+// rotated until orthogonal while the rotations accumulate in J:
+//   J R = D Y   =>   X = Q J^H D Y.
+// Wide A = X^H = Y^H D J Q^H:  U = Y^H, S = D, VH = J Q^H.
+// Tall A = X  = (Q J^H) D Y:   U = Q J^H, S = D, VH = Y.
+// Both factors come out orthonormal for every singular value (the normalised
+// rows Y and the accumulated J are unitary by construction), the Jacobi
+// works on nr x nr instead of nr x L rows, and the triangular start needs far
+// fewer sweeps on graded matrices than A itself.
 template <typename T>
 static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typename traits<T>::real* S, T* VH,
                     int max_sweeps, double tol, void* work, size_t wb, int* info, cudaStream_t st) {
@@ -192,7 +209,7 @@ static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typenam
   const int tall = m > n;
   const int64_t nr = tall ? n : m, L = tall ? m : n;
   if (tol <= 0) {
-    double sl = sqrt((double)(L > 8 ? L : 8));
+    double sl = sqrt((double)(nr > 8 ? nr : 8));
     tol = sl * traits<T>::eps * (sizeof(R) == 4 ? 4.0 : 1.0);
   }
   char* w = (char*)work;
@@ -202,21 +219,20 @@ static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typenam
   int64_t* pos = (int64_t*)(w + Ly.pos);
   unsigned* counters = (unsigned*)(w + Ly.counters);
   SyncWords* sw = (SyncWords*)(w + Ly.sync);
-  int s;
-  if (tall) {  // W = A^H (n x m)
-    int64_t shp[2] = {m, n};
-    int perm[2] = {1, 0};
-    s = tnc_permute(dtype_of<T>(), A, W, 2, shp, perm, 1, st);
-  } else {
-    s = cudaMemcpyAsync(W, A, (size_t)m * n * sizeof(T), cudaMemcpyDeviceToDevice, st) == cudaSuccess ? TNC_OK
-                                                                                                       : TNC_ERR_CUDA;
-  }
+  double* frob2 = (double*)(w + Ly.frob2);
+  T* Qt = nullptr;
+  // X = A^H (wide) or A (tall); R of X into W, Q^T (nr x L) kept in the QR workspace
+  int s = qr_qt<T>(L, nr, A, tall ? 0 : 1, true, W, w + Ly.qr, qr_qt_workspace(L, nr, sizeof(T)), info, st, &Qt);
   if (s) return s;
+  T* small = (T*)(w + Ly.qr);  // the QR's transposed copy (nr * L >= nr * nr elements) is free now
   eye_kernel<T><<<grid1d(nr * nr, 256), 256, 0, st>>>(J, nr);
   if (cudaMemsetAsync(counters, 0, kMaxSweepsCap * sizeof(unsigned), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
-  if (cudaMemsetAsync(info, 0, 4 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
-  if (launch_status()) return TNC_ERR_CUDA;
+  // info[0] holds the QR's status (a wait timeout) until the Jacobi writes its own
+  if (cudaMemsetAsync(info + 1, 0, 3 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(frob2, 0, sizeof(double), st) != cudaSuccess) return TNC_ERR_CUDA;
+  frob2_kernel<T><<<grid1d(nr * nr, 256, 152 * 4), 256, 0, st>>>(nr * nr, W, frob2);
+  if (launch_status(2)) return TNC_ERR_CUDA;  // eye, frob2
   if (nr > 1) {
     const int threads = kSvdWarps * 32;
     int cap = coop_capacity((const void*)jacobi_kernel<T>, threads, 0);
@@ -224,21 +240,27 @@ static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typenam
     int64_t npairs = (nr + 1) / 2;
     int64_t want = (npairs + kSvdWarps - 1) / kSvdWarps;
     int grid = (int)(want < cap ? want : cap);
-    int64_t nr_ = nr, L_ = L;
+    int64_t nr_ = nr, L_ = nr;
     int ms = max_sweeps;
     double tl = tol;
     void* args[] = {(void*)&W, (void*)&J, (void*)&nr_, (void*)&L_, (void*)&ms, (void*)&tl,
-                    (void*)&counters, (void*)&sw, (void*)&info};
+                    (void*)&frob2, (void*)&counters, (void*)&sw, (void*)&info};
     if (cudaLaunchCooperativeKernel((const void*)jacobi_kernel<T>, dim3(grid), dim3(threads), args, 0, st) !=
         cudaSuccess)
       return TNC_ERR_CUDA;
   }
   copy_sync_error<<<1, 1, 0, st>>>(sw, info);
-  row_norms_kernel<T><<<grid1d(nr * 32, 256), 256, 0, st>>>(W, nr, L, D, info);
+  row_norms_kernel<T><<<grid1d(nr * 32, 256), 256, 0, st>>>(W, nr, nr, D, info);
   rank_kernel<R><<<grid1d(nr, 128), 128, 0, st>>>(D, nr, pos);
-  svd_output_kernel<T><<<grid1d(nr * L, 256), 256, 0, st>>>(W, J, D, pos, nr, L, tall, U, S, VH);
-  // [jacobi], error copy, row norms, rank, output
-  return launch_status(nr > 1 ? 5 : 4);
+  // the square problem's factors: wide -> U = Y^H (out), J -> small; tall -> VH = Y (out), J^H -> small
+  if (tall) svd_output_kernel<T><<<grid1d(nr * nr, 256), 256, 0, st>>>(W, J, D, pos, nr, nr, 0, small, S, VH);
+  else svd_output_kernel<T><<<grid1d(nr * nr, 256), 256, 0, st>>>(W, J, D, pos, nr, nr, 1, U, S, small);
+  if (launch_status(nr > 1 ? 4 : 3)) return TNC_ERR_CUDA;  // [jacobi], error copy, row norms, rank, output
+  const T one = one_<T>(), zero = zero_<T>();
+  if (tall)  // U (m x n) = Q (small) = (Q^T)^T small
+    return gemm_launch<T>(TNC_OP_T, TNC_OP_N, L, nr, nr, one, Qt, L, 0, small, nr, 0, zero, U, nr, 0, 1, st);
+  // VH (m x n) = small Q^H = small conj(Q^T)
+  return gemm_launch<T>(TNC_OP_N, TNC_OP_R, nr, L, nr, one, small, nr, 0, Qt, L, 0, zero, VH, L, 0, 1, st);
 }
 
 }  // namespace tnc
@@ -274,8 +296,8 @@ extern "C" int tnc_svd(int dtype, int64_t m, int64_t n, const void* A, int64_t l
 // the process exits, and no call allocates or frees device memory.
 //
 // Limit: the problem's workspace (tnc_svd_workspace_size) must fit in
-// kNoAllocScratchBytes = 16 MiB, e.g. complex128 up to 512 x 768 or
-// complex64 up to 768 x 1024; larger problems are rejected with
+// kNoAllocScratchBytes = 16 MiB, e.g. complex128 up to 448 x 512 or
+// complex64 up to 512 x 1024; larger problems are rejected with
 // TNC_ERR_TOO_LARGE before anything is launched.
 //
 // All calls on a device share the one scratch area and it keeps whatever the

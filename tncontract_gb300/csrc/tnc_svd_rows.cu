@@ -44,11 +44,12 @@ struct Rot {
 // Jacobi rotation from the 2x2 Gram entries (see tnc_svd.cu for the formula)
 template <typename T>
 __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename traits<T>::real b, T g,
-                                           typename traits<T>::real rtol) {
+                                           typename traits<T>::real rtol, typename traits<T>::real noise2) {
   typedef typename traits<T>::real R;
   Rot<T> r;
-  const R h = sqrt(abs2_(g));
-  r.apply = (h > rtol * sqrt(a) * sqrt(b));
+  const R h = abs_(g);
+  // rows at the rounding-noise floor (or whose squared norm underflowed) count as converged
+  r.apply = (a > noise2) && (b > noise2) && (a > 0) && (b > 0) && (h > rtol * sqrt(a) * sqrt(b));
   if (!r.apply) { r.c = 1; r.se = zero_<T>(); r.sec = zero_<T>(); return r; }
   const R tau = (b - a) / (2 * h);
   R t;
@@ -56,7 +57,7 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
   else t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
   r.c = R(1) / sqrt(R(1) + t * t);
   const R s = r.c * t;
-  const T e = g * (R(1) / h);
+  const T e = div_real_(g, h);
   r.se = s * e;
   r.sec = s * conj_(e);
   return r;
@@ -64,7 +65,8 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
 
 // rows x (registers, MAXE per lane) and y (shared memory), one warp
 template <typename T, int MAXE>
-__device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, typename traits<T>::real rtol) {
+__device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, typename traits<T>::real rtol,
+                                                typename traits<T>::real noise2) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
   R a = 0, b = 0;
@@ -84,7 +86,7 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
   a = warp_sum(a);
   b = warp_sum(b);
   g = warp_sum(g);
-  const Rot<T> r = make_rot<T>(a, b, g, rtol);
+  const Rot<T> r = make_rot<T>(a, b, g, rtol, noise2);
   if (!r.apply) return false;
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
@@ -98,7 +100,8 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
 
 // rows x and y both in shared memory, one warp
 template <typename T>
-__device__ __forceinline__ bool rotate_smem_smem(T* x, T* y, int64_t L, typename traits<T>::real rtol) {
+__device__ __forceinline__ bool rotate_smem_smem(T* x, T* y, int64_t L, typename traits<T>::real rtol,
+                                                 typename traits<T>::real noise2) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
   R a = 0, b = 0;
@@ -112,7 +115,7 @@ __device__ __forceinline__ bool rotate_smem_smem(T* x, T* y, int64_t L, typename
   a = warp_sum(a);
   b = warp_sum(b);
   g = warp_sum(g);
-  const Rot<T> r = make_rot<T>(a, b, g, rtol);
+  const Rot<T> r = make_rot<T>(a, b, g, rtol, noise2);
   if (!r.apply) return false;
   for (int64_t k = lane; k < L; k += 32) {
     const T xv = x[k], yv = y[k];
@@ -151,8 +154,8 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
 
 template <typename T, int MAXE>
 __global__ void __launch_bounds__(256)
-jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, unsigned* counters,
-                    SyncWords* sw, int* info) {
+jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
+                    unsigned* counters, SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sB = reinterpret_cast<T*>(smem_raw);
@@ -161,6 +164,7 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
   const int64_t nbp = nb + (nb & 1);
   const int64_t ntask = nbp / 2;
   const R rtol = (R)tol;
+  const R noise2 = noise_floor2<T>(frob2);
   int sweep = 0;
   bool converged = false;
   unsigned last_rot = 0;
@@ -178,7 +182,7 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
         if (warp < hp / 2) {
           int64_t p, q;
           circle_pair(hp, rr, warp, p, q);
-          if (p < cnt && q < cnt) rot += rotate_smem_smem(sB + p * L, sB + q * L, L, rtol) ? 1u : 0u;
+          if (p < cnt && q < cnt) rot += rotate_smem_smem(sB + p * L, sB + q * L, L, rtol, noise2) ? 1u : 0u;
         }
         __syncthreads();
       }
@@ -207,7 +211,7 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
         __syncthreads();
         for (int s = 0; s < h; ++s) {
           const int j = (warp + s) % h;
-          if (hasA && j < cntB) rot += rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol) ? 1u : 0u;
+          if (hasA && j < cntB) rot += rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol, noise2) ? 1u : 0u;
           __syncthreads();
         }
         if (hasA) {
@@ -287,12 +291,13 @@ __global__ void gather_rows_kernel(const T* src, int64_t L, const int64_t* order
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-struct RowsLayout { size_t d, counters, sync, total; };
+struct RowsLayout { size_t d, frob2, counters, sync, total; };
 static const int kRowsMaxSweeps = 100;
 static RowsLayout rows_layout(int64_t nr, size_t rs) {
   RowsLayout Ly;
   size_t off = 0;
   Ly.d = off; off = align256(off + (size_t)nr * rs);
+  Ly.frob2 = off; off = align256(off + sizeof(double));
   Ly.counters = off; off = align256(off + kRowsMaxSweeps * sizeof(unsigned));
   Ly.sync = off; off = align256(off + sizeof(SyncWords));
   Ly.total = off;
@@ -325,8 +330,8 @@ static int ensure_smem_attr() {
 }
 
 template <typename T, int MAXE>
-static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, unsigned* counters, SyncWords* sw,
-                        int* info, cudaStream_t st) {
+static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, const double* frob2,
+                        unsigned* counters, SyncWords* sw, int* info, cudaStream_t st) {
   const size_t smem = (size_t)h * L * sizeof(T);
   const void* fn = (const void*)jacobi_block_kernel<T, MAXE>;
   if (smem > kMaxHalfBlockBytes) return TNC_ERR_ARG;
@@ -345,7 +350,7 @@ static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, 
   int h_ = h, ms_ = ms;
   double tol_ = tol;
   void* args[] = {(void*)&W, (void*)&nr_, (void*)&L_, (void*)&h_, (void*)&ms_, (void*)&tol_,
-                  (void*)&counters, (void*)&sw, (void*)&info};
+                  (void*)&frob2, (void*)&counters, (void*)&sw, (void*)&info};
   if (cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, st) != cudaSuccess) return TNC_ERR_CUDA;
   return TNC_OK;
 }
@@ -367,6 +372,7 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
   R* D = (R*)(w + Ly.d);
   unsigned* counters = (unsigned*)(w + Ly.counters);
   SyncWords* sw = (SyncWords*)(w + Ly.sync);
+  double* frob2 = (double*)(w + Ly.frob2);
   int s;
   if (tall) {
     int64_t shp[2] = {m, n};
@@ -382,6 +388,9 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
   if (cudaMemsetAsync(info, 0, 4 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
   int launched = 0;
   if (nr > 1) {
+    if (cudaMemsetAsync(frob2, 0, sizeof(double), st) != cudaSuccess) return TNC_ERR_CUDA;
+    frob2_kernel<T><<<grid1d(nr * L, 256, 152 * 4), 256, 0, st>>>(nr * L, W, frob2);
+    ++launched;
     // half-block height: 16 rows (fewest barriers) when the shared-memory half
     // block and the register row fit, else smaller
     int h = 8;
@@ -390,12 +399,12 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
     while (h > 2 && h / 2 >= nr) h >>= 1;
     const bool big = sizeof(T) >= 16;
     int rc;
-    if (L <= 256) rc = launch_block<T, 8>(W, nr, L, h, max_sweeps, tol, counters, sw, info, st);
-    else if (L <= 512) rc = launch_block<T, 16>(W, nr, L, h, max_sweeps, tol, counters, sw, info, st);
-    else if (L <= 1024 && !big) rc = launch_block<T, 32>(W, nr, L, h, max_sweeps, tol, counters, sw, info, st);
+    if (L <= 256) rc = launch_block<T, 8>(W, nr, L, h, max_sweeps, tol, frob2, counters, sw, info, st);
+    else if (L <= 512) rc = launch_block<T, 16>(W, nr, L, h, max_sweeps, tol, frob2, counters, sw, info, st);
+    else if (L <= 1024 && !big) rc = launch_block<T, 32>(W, nr, L, h, max_sweeps, tol, frob2, counters, sw, info, st);
     else return TNC_ERR_ARG;  // rows too long for the register-resident half block
     if (rc) return rc;
-    launched = 1;
+    ++launched;
   }
   copy_sync_error<<<1, 1, 0, st>>>(sw, info);
   rows_norm_kernel<T><<<grid1d(nr * 32, 256), 256, 0, st>>>(W, nr, L, D, info);

@@ -15,9 +15,11 @@ option:
   pipe of GB300 is 64x its FP64 pipe).  Fidelity error against the FP64
   result is reported by the benchmark and checked by the tests.
 
-The truncating SVD of each site uses the block one-sided Jacobi of
-``tnc_svd_rows`` (rotations not accumulated) and recovers the second factor
-with one GEMM.  ``apply_compress_batch`` runs several instances at once, one
+The truncating SVD of each site factors M^H = Q R (R only, ``tnc_qr_r``),
+runs the block one-sided Jacobi of ``tnc_svd_rows`` on the rows of R
+(rotations not accumulated; the rotated rows are S U^H of M) and forms
+S V^H = U^H M with one GEMM.  Directions at the storage type's rounding-noise
+floor are never kept (``noise_rank``).  ``apply_compress_batch`` runs several instances at once, one
 CUDA stream and one host thread each (the native calls release the GIL), so
 the per-site latency chains of different instances overlap on the GPU.
 """
@@ -120,33 +122,37 @@ def _check_info(info):
 
 
 def _factor_full(M):
-    """Full SVD of M (m x n) -> (S device, S host, factors(k) -> (U_k, SV_k)).
-    Rows up to the register limit use the non-accumulating block Jacobi;
-    longer rows use the accumulating SVD."""
+    """Full SVD of M (m x n) -> (S device, factors(k) -> (U_k, SV_k)).
+
+    Columns up to the register limit (m rows) use the QR-preconditioned,
+    non-accumulating block Jacobi: M^H = Q R, the rows of R (min(m, n) x m)
+    are orthogonalised, which leaves them equal to S U^H of M (M = R^H Q^H),
+    so U is the normalised rows and S V^H = U^H M is one GEMM.  U is then
+    orthonormal to the Jacobi tolerance for every kept direction, however
+    small its singular value (recovering U = M V / S instead divides the
+    Jacobi's residual non-orthogonality by s_j and fails for spectra that
+    fall below the storage precision), and the triangular start needs fewer
+    sweeps on graded matrices (Drmac & Veselic 2008).  Longer columns run
+    the accumulating SVD on the same R (its VH rows are then U^H of M)."""
     m, n = M.shape
-    if max(m, n) <= _rows_limit(M.dtype):
-        W, S, order, info = _ops.svd_rows(M)
+    R = _ops.qr_r(M, adjoint=True)                                         # min(m, n) x m
+    if m <= _rows_limit(M.dtype):
+        W, S, order, info = _ops.svd_rows(R)                               # W rows = S U^H
         _check_info(info)
 
         def factors(k, kdev):
-            if m <= n:  # W rows = S V^H
-                SV = _ops.gather_rows(W, order, kdev, k, mode=0)          # k x n
-                U = _ops.empty((m, k), M.dtype)
-                _ops.gemm(L.OP_N, L.OP_C, m, k, n, M, n, SV, n, U, k)     # M (S V^H)^H
-                _ops.scale_cols(U, S[:k].contiguous(), 3)                  # / S^2
-            else:       # W rows = S U^H
-                U = _ops.gather_rows(W, order, kdev, k, S=S, mode=1)      # m x k
-                SV = _ops.empty((k, n), M.dtype)
-                _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)     # U^H M
+            U = _ops.gather_rows(W, order, kdev, k, S=S, mode=1)          # m x k
+            SV = _ops.empty((k, n), M.dtype)
+            _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)         # U^H M
             return U, SV
         return S, factors
-    U, S, VH = _ops.svd(M)
+    _u, S, VH = _ops.svd(R)                                                # VH rows = U^H of M
 
     def factors(k, kdev):
-        Uk = _ops.slice_last(U, k) if k < U.shape[1] else U
-        SV = VH[:k].contiguous().clone()
-        _ops.scale_rows(SV, S[:k].contiguous(), 0)
-        return Uk, SV
+        U = _ops.permute(VH[:k].contiguous(), (1, 0), conj=True)          # m x k
+        SV = _ops.empty((k, n), M.dtype)
+        _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)             # U^H M
+        return U, SV
     return S, factors
 
 
@@ -183,6 +189,30 @@ def _factor_sketch(M, l, power_iters, seed):
         _ops.gemm(L.OP_N, L.OP_N, m, k, l, Q, l, UB, k, U, k)
         return U, SV
     return S, factors, residual
+
+
+def reference_rank(s, chi, threshold):
+    """The reference's truncation rule on descending singular values s: keep
+    s / s_max > threshold, then at most chi (onedim_core.py:332-339)."""
+    if s.size == 0 or s[0] <= 0:
+        return 0
+    k = int(np.count_nonzero(s > threshold * s[0]))
+    return min(k, chi) if chi else k
+
+
+_EPS = {torch.float32: 2.0 ** -23, torch.complex64: 2.0 ** -23,
+        torch.float64: 2.0 ** -52, torch.complex128: 2.0 ** -52}
+
+
+def noise_rank(s, dtype):
+    """Number of singular values above the rounding-noise floor of the
+    storage type, 4 eps |M|_F.  The Jacobi stages leave rows at or below
+    eps |M|_F out of their rotations (their directions are rounding noise),
+    so directions there are never kept, whatever the rank rule asks (in FP64
+    the floor sits below the reference's 1e-14 threshold for all but very
+    flat spectra)."""
+    floor = 4.0 * _EPS[dtype] * float(np.sqrt(np.sum(s ** 2)))
+    return max(1, int(np.count_nonzero(s > floor))) if s.size and s[0] > 0 else 0
 
 
 class RankStats:
@@ -232,6 +262,7 @@ def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None,
                     used_sketch = True
                     # rank by the same rule, the uncaptured weight counted as discarded
                     k = RM.dw_rank(s_host, dw_tol, chi or 0, total=float((s_host ** 2).sum()) + residual)
+                    k = min(k, noise_rank(s_host, M.dtype))
                     smax = float(s_host[0])
                     disc = float((s_host[k:] ** 2).sum()) + residual
                     kd = torch.tensor([k], dtype=torch.int64, device=M.device)
@@ -242,18 +273,15 @@ def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None,
                     rank_stats.fallbacks += 1
         if not used_sketch:
             S, factors = _factor_full(M)
+            s_host = S.cpu().numpy().astype(np.float64)
             if dw_tol is None:
-                kdev = []
-                k, disc, smax = _ops.truncation_rank(S, chi or 0, threshold, relative=True, with_smax=True,
-                                                     kdev_out=kdev)
-                kd = kdev[0]
-                s_host = None
+                k = reference_rank(s_host, chi or 0, threshold)
             else:
-                s_host = S.cpu().numpy().astype(np.float64)
                 k = RM.dw_rank(s_host, dw_tol, chi or 0)
-                smax = float(s_host[0])
-                disc = float((s_host[k:] ** 2).sum())
-                kd = torch.tensor([k], dtype=torch.int64, device=M.device)
+            k = min(k, noise_rank(s_host, M.dtype))
+            smax = float(s_host[0])
+            disc = float((s_host[k:] ** 2).sum())
+            kd = torch.tensor([k], dtype=torch.int64, device=M.device)
             if rank_stats is not None:
                 rank_stats.full += 1
                 rank_stats.rows_factored += kmax * kmax * max(m, n)
@@ -263,7 +291,7 @@ def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None,
         if smax == 0.0:
             raise ValueError("zero state in the SVD sweep")
         if rank_stats is not None or rank_model is not None:
-            s_prev = s_host if s_host is not None else S.cpu().numpy().astype(np.float64)
+            s_prev = s_host
         U, SV = factors(k, kd)
         P[i] = _ops.permute(U.reshape(d, r, k), (0, 2, 1))             # (phys, k, right)
         dp, lp, rp = P[i - 1].shape                                      # rp == l
@@ -309,6 +337,115 @@ def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0
         stats.log_norm = total
         stats.norm_folded = folded
     return P
+
+
+def compress(sites, chi, threshold=1e-15, stats=None, log_norm_in=0.0, fold_norm=True):
+    """``MatrixProductState.svd_compress(chi, threshold)`` on (phys, left,
+    right) device sites (no MPO).  Returns (sites, log_norm): the state is
+    exp(log_norm) times the returned sites; with ``fold_norm`` the factor is
+    folded into the first site when it is representable (log_norm is then 0)."""
+    P = [s for s in sites]
+    log_norm = qr_left_sweep(P) + log_norm_in
+    norm_acc = svd_right_sweep(P, chi, threshold, stats)
+    if norm_acc > 0:
+        log_norm += float(np.log(norm_acc))
+        P[0] = _ops.scale(P[0], 1.0 / norm_acc)   # keep the returned sites normalised
+    if fold_norm and abs(log_norm) <= _FOLD_LIMIT.get(P[0].dtype, 600.0):
+        P[0] = _ops.scale(P[0], float(np.exp(log_norm)))
+        log_norm = 0.0
+    return P, log_norm
+
+
+def run_batch(jobs, streams=None):
+    """Run callables concurrently, each on its own CUDA stream and host
+    thread (the native calls release the GIL); returns their results."""
+    B = len(jobs)
+    if streams is None:
+        streams = [torch.cuda.Stream() for _ in range(B)]
+    out = [None] * B
+    errs = [None] * B
+    dev = torch.cuda.current_device()
+    cur = torch.cuda.current_stream()
+
+    def run(b):
+        try:
+            torch.cuda.set_device(dev)
+            streams[b % len(streams)].wait_stream(cur)
+            with torch.cuda.stream(streams[b % len(streams)]):
+                out[b] = jobs[b]()
+        except BaseException as e:
+            errs[b] = e
+
+    threads = [threading.Thread(target=run, args=(b,)) for b in range(B)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for e in errs:
+        if e is not None:
+            raise e
+    for s in streams:
+        cur.wait_stream(s)
+    return out
+
+
+def boundary_mps_contract(layer, chi, threshold=1e-14, precision="fp32"):
+    """``SquareLatticeTensorNetwork.mps_contract`` with SVD compression
+    (tncontract/twodim/square_lattice.py:130-203) on the engine: ``layer``
+    is a 2-D list of double-layer tensors with legs (down, left, right, up)
+    (device or host arrays).  Every site is balanced to unit norm, the
+    column MPS is normalised after each compression and all scale factors are
+    summed as natural logarithms on the host (the reference keeps the running
+    norm in np.longdouble for the same reason: the 8x8 norm network is
+    ~1e115, beyond FP32).  Returns (value as a Python complex or float when
+    representable else None, log10 |value|, phase)."""
+    nrows, ncols = len(layer), len(layer[0])
+    first = layer[0][0]
+    cplx = first.is_complex() if isinstance(first, torch.Tensor) else bool(np.iscomplexobj(first))
+    dt = compute_dtype(precision, cplx)
+    log_total = 0.0
+
+    def prep(t, perm):
+        a = _ops.to_device(t)
+        n = _ops.nrm2(a)
+        a = _ops.scale(a, 1.0 / n) if n > 0 else a
+        return _ops.cast(_ops.permute(a, perm).contiguous(), dt), (float(np.log(n)) if n > 0 else 0.0)
+
+    # column 0 -> MPS (phys=right, left=up, right=down); dummy 'left' leg dropped
+    mps = []
+    for i in range(nrows):
+        t = layer[i][0]
+        a, ln = prep(t, (2, 3, 0, 1))       # (right, up, down, left[1])
+        mps.append(a.reshape(a.shape[0], a.shape[1], a.shape[2]))
+        log_total += ln
+    mps, ln = compress(mps, chi, threshold, fold_norm=False)
+    log_total += ln
+    for c in range(1, ncols - 1):
+        mpo = []
+        for i in range(nrows):
+            a, ln = prep(layer[i][c], (2, 1, 3, 0))   # (physout=right, physin=left, up, down)
+            mpo.append(a)
+            log_total += ln
+        mps = apply_mpo(mps, mpo)
+        mps, ln = compress(mps, chi, threshold, fold_norm=False)
+        log_total += ln
+    last = []
+    for i in range(nrows):
+        a, ln = prep(layer[i][ncols - 1], (1, 3, 0, 2))  # (left, up, down, right[1])
+        last.append(a.reshape(a.shape[0], a.shape[1], a.shape[2]))
+        log_total += ln
+    v = inner_product(mps, last, conj_bra=False)
+    mag = abs(v)
+    if mag == 0:
+        return 0.0, float("-inf"), 1.0
+    log10 = (log_total + math.log(mag)) / math.log(10.0)
+    phase = v / mag
+    value = None
+    if abs(log10) < 300:
+        value = phase * 10.0 ** log10
+        if not cplx:
+            value = value.real
+    return value, log10, phase
 
 
 def apply_compress_batch(batch, mpo, chi, threshold=1e-15, streams=None, stats=None, log_norms=None):

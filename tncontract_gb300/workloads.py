@@ -85,6 +85,36 @@ def random_peps_arrays(seed, nrows, ncols, D, d, dtype=np.float64):
     return rows
 
 
+def config3_specs(seed=1, count=512):
+    """The uneven batch: per instance N ~ U{16..128}, d ~ {2, 3, 4},
+    chi ~ U{16..256}, dtype alternating float32 / complex64 (drawn in this
+    order from one generator); the instance's sites use seed (seed*100000 + b)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for b in range(count):
+        N = int(rng.integers(16, 129))
+        d = int(rng.choice([2, 3, 4]))
+        chi = int(rng.integers(16, 257))
+        specs.append((N, d, chi, np.complex64 if b % 2 else np.float32, seed * 100000 + b))
+    return specs
+
+
+def double_layer_arrays(peps_rows):
+    """Double-layer norm tensors conj(ket).ket over phys with legs
+    (down, left, right, up), each the bra-major fusion of the two layers
+    (inner_product_peps + consolidate_indices, square_lattice.py:283-304)."""
+    out = []
+    for row in peps_rows:
+        r = []
+        for k in row:
+            t = np.tensordot(np.conj(k), k, (0, 0))  # (u,r,dn,l | u,r,dn,l)
+            u, rr, dn, lf = k.shape[1:]
+            t = t.transpose(2, 6, 3, 7, 1, 5, 0, 4).reshape(dn * dn, lf * lf, rr * rr, u * u)
+            r.append(np.ascontiguousarray(t))
+        out.append(r)
+    return out
+
+
 def sweep_flops(N, d, D, chi, complex_=True, chi_in=None):
     """Algorithmic flops of one apply + svd_compress sweep (fixed count,
     implementation independent), from the bond dimensions the plain method
