@@ -67,13 +67,15 @@ def _arr(ctype, seq):
 
 # When set to a dict, every C-ABI call is bracketed by CUDA events on the
 # current stream: PROFILE[name] -> list of (start, end, algorithmic flops).
+# PROFILE_ONLY (a set of names) restricts the bracketing to those calls.
 PROFILE = None
+PROFILE_ONLY = None
 
 
 def _call(name, *args, flops=0.0):
     fn = getattr(L.lib(), name)
     prof = PROFILE
-    if prof is None:
+    if prof is None or (PROFILE_ONLY is not None and name not in PROFILE_ONLY):
         L.check(name, fn(*args))
         return
     s = torch.cuda.Event(enable_timing=True)
