@@ -85,7 +85,8 @@ def test_gemm_batched_alpha_beta(gpu):
 
 
 @pytest.mark.parametrize("dt", DTYPES)
-@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (6, 6), (40, 13), (13, 40), (130, 97), (256, 512)])
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (6, 6), (40, 13), (13, 40), (130, 97), (256, 512),
+                                   (700, 300), (300, 700), (1536, 768)])
 def test_qr(gpu, dt, shape):
     from tncontract_gb300 import _ops
     rng = np.random.default_rng(4)
@@ -106,7 +107,7 @@ def test_qr(gpu, dt, shape):
 
 
 @pytest.mark.parametrize("dt", DTYPES)
-@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (40, 13), (13, 40), (256, 512), (700, 300)])
+@pytest.mark.parametrize("shape", [(1, 1), (1, 7), (7, 1), (40, 13), (13, 40), (256, 512), (700, 300), (512, 768)])
 def test_qr_r_only(gpu, dt, shape):
     """tnc_qr_r: R of A and of A^H equal the R of the full QR of the same
     matrix (same reflectors, Q not formed)."""

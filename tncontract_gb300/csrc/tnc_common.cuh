@@ -176,8 +176,8 @@ int gemm_launch(int opA, int opB, int64_t m, int64_t n, int64_t k, T alpha,
 // Householder QR of X (fm x fn): X = A (adjoint = 0, A dense fm x fn) or
 // X = A^H (adjoint = 1, A dense fn x fm).  Writes R (min(fm,fn) x fn); with
 // want_qt also forms Q^T (min(fm,fn) x fm, row-major) inside the workspace
-// and returns its address in *qt.  Workspace: qr_qt_workspace(fm, fn, es).
-size_t qr_qt_workspace(int64_t fm, int64_t fn, size_t es);
+// and returns its address in *qt.  Workspace: qr_qt_workspace(fm, fn, dtype).
+size_t qr_qt_workspace(int64_t fm, int64_t fn, int dtype);
 template <typename T>
 int qr_qt(int64_t fm, int64_t fn, const T* A, int adjoint, bool want_qt, T* R, void* work, size_t wb, int* info,
           cudaStream_t st, T** qt);

@@ -17,6 +17,8 @@
 // H_{min(j,k-1)} ... H_0 to its own column e_j -- independent across warps.
 #include "tnc_persist.cuh"
 
+#include <atomic>
+
 namespace tnc {
 
 constexpr int kQrWarps = 4;  // warps per CTA
@@ -72,7 +74,7 @@ __device__ __forceinline__ void apply_reflector_h(T* col, const T* v, T tau, int
 
 template <typename T>
 __global__ void __launch_bounds__(kQrWarps * 32)
-qr_factor_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) {
+qr_factor_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, SyncWords* sw) {
   const int64_t k = m < n ? m : n;
   const int64_t nwarps = (int64_t)gridDim.x * kQrWarps;
   const int64_t wid = (int64_t)blockIdx.x * kQrWarps + (threadIdx.x >> 5);
@@ -90,12 +92,12 @@ qr_factor_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw)
     while (first <= c) first += nwarps;
     if (first >= n) break;  // nothing left to update
     if (!warp_wait_flag(&flags[c], sw)) return;
-    const T* v = Bt + c * m;
+    const T* v = Bt + c * ld;
     const T tc = ldcg(tau + c);
     for (int64_t j = first; j < n; j += nwarps) {
-      apply_reflector_h(Bt + j * m, v, tc, c, m);
+      apply_reflector_h(Bt + j * ld, v, tc, c, m);
       if (j == c + 1 && j < k) {  // look-ahead: publish the next reflector now
-        make_reflector(Bt + j * m, j, m, tau + j);
+        make_reflector(Bt + j * ld, j, m, tau + j);
         __threadfence();
         if (lane == 0) atomicExch(&flags[j], 1);
       }
@@ -222,7 +224,7 @@ __device__ __forceinline__ void apply_reg(T (&x)[E], const T (&vv)[E], T tau, in
 
 template <typename T, int E>
 __global__ void __launch_bounds__(kPanel * 32)
-qr_panel_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) {
+qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, SyncWords* sw) {
   __shared__ T sv[32 * E];
   __shared__ T stau;
   const int64_t k = m < n ? m : n;
@@ -236,7 +238,7 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) 
 #pragma unroll
     for (int u = 0; u < E; ++u) {
       const int64_t i = lane + 32 * u;
-      x[u] = (i < m) ? Bt[j * m + i] : zero_<T>();
+      x[u] = (i < m) ? Bt[j * ld + i] : zero_<T>();
     }
   }
   // reflectors of earlier panels, as they are published
@@ -247,7 +249,7 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) 
 #pragma unroll
       for (int u = 0; u < E; ++u) {
         const int64_t i = lane + 32 * u;
-        vv[u] = (i > c && i < m) ? ldcg(Bt + c * m + i) : zero_<T>();
+        vv[u] = (i > c && i < m) ? ldcg(Bt + c * ld + i) : zero_<T>();
       }
       apply_reg(x, vv, ldcg(tau + c), c, m);
     }
@@ -265,7 +267,7 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) 
         const int64_t i = lane + 32 * u;
         if (i < m) {
           sv[i] = x[u];
-          if (i >= c) stcg(Bt + c * m + i, x[u]);
+          if (i >= c) stcg(Bt + c * ld + i, x[u]);
         }
       }
       if (lane == 0) {
@@ -291,7 +293,7 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, T* tau, int* flags, SyncWords* sw) 
 #pragma unroll
     for (int u = 0; u < E; ++u) {
       const int64_t i = lane + 32 * u;
-      if (i < m) Bt[j * m + i] = x[u];
+      if (i < m) Bt[j * ld + i] = x[u];
     }
   }
 }
@@ -325,25 +327,239 @@ qr_form_q_reg_kernel(const T* __restrict__ Bt, int64_t m, int64_t k, const T* __
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// ---------------------------------------------------------------------------
+// Blocked factorisation (the geqrf / ungqr structure with compact-WY block
+// reflectors, Schreiber & Van Loan 1989).  Panels of kQrNB columns are factored
+// by the dataflow kernels above on the panel's sub-matrix; then, with
+//   H_c0 ... H_c0+nb-1 = I - V T V^H        (T upper triangular, larft),
+// the trailing columns get A2 <- (I - V T^H V^H) A2 and Q is formed backwards,
+// Q <- (I - V T V^H) Q for the panels in reverse order.  In the transposed
+// working layout (rows of Bt / Qt are columns of A / Q) each update is
+//   Wt = X2t conj(V) ,  W2t = Wt op(T) ,  X2t -= W2t Vt
+// with the long dimension as GEMM rows.  FP32-class types run these GEMMs on
+// the tensor cores (TF32 split products, FP32-class accuracy), FP64 types on
+// the CUDA-core GEMM.
+template <typename T>
+static int dtype_of() {
+  return sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128);
+}
+
+constexpr int64_t kQrNB = 64;
+constexpr int64_t kQrBlockedMin = 2 * kQrNB;  // k below this: unblocked dataflow only
+
+constexpr int64_t kQrSplitK = 128;  // K chunk of the split-K products
+
 struct QrLayout {
-  size_t bt, tau, flags, sync, qt, total;
+  size_t bt, tau, flags, sync, qt, vt, s, tm, wt, w2t, part, tcws, tcws_bytes, total;
+  bool blocked;
 };
-static QrLayout qr_layout(int64_t m, int64_t n, size_t es) {
+static QrLayout qr_layout(int64_t m, int64_t n, int dt) {
+  const size_t es = (size_t)elem_size(dt);
   int64_t k = m < n ? m : n;
   QrLayout L;
   size_t off = 0;
+  L.blocked = k >= kQrBlockedMin;
   L.bt = off; off = align256(off + (size_t)n * m * es);
   L.tau = off; off = align256(off + (size_t)k * es);
   L.flags = off; off = align256(off + (size_t)k * sizeof(int));
   L.sync = off; off = align256(off + sizeof(SyncWords));
   L.qt = off; off = align256(off + (size_t)k * m * es);
+  L.vt = L.s = L.tm = L.wt = L.w2t = L.part = L.tcws = off;
+  L.tcws_bytes = 0;
+  if (L.blocked) {
+    const int64_t nblk = (k + kQrNB - 1) / kQrNB;
+    const int64_t rows = n > k ? n : k;
+    L.vt = off; off = align256(off + (size_t)kQrNB * m * es);
+    L.s = off; off = align256(off + (size_t)kQrNB * kQrNB * es);
+    L.tm = off; off = align256(off + (size_t)nblk * kQrNB * kQrNB * es);
+    L.wt = off; off = align256(off + (size_t)rows * kQrNB * es);
+    L.w2t = off; off = align256(off + (size_t)rows * kQrNB * es);
+    L.part = off; off = align256(off + (size_t)((m + kQrSplitK - 1) / kQrSplitK) * rows * kQrNB * es);
+    if (dt == TNC_F32 || dt == TNC_C64) {  // tensor-core GEMMs: split-operand workspace
+      size_t a = 0, b = 0;
+      tnc_gemm_tc_workspace_size(dt, rows, kQrNB, m, 1, &a);
+      tnc_gemm_tc_workspace_size(dt, rows, m, kQrNB, 1, &b);
+      L.tcws_bytes = a > b ? a : b;
+    }
+    L.tcws = off; off = align256(off + L.tcws_bytes);
+  }
   L.total = off;
   return L;
 }
 
+// Vt[j][i] = reflector j of a panel (i = row within the panel's sub-matrix):
+// 0 above the diagonal, 1 on it, the stored entries below
 template <typename T>
-static int dtype_of() {
-  return sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128);
+__global__ void qr_extract_vt(const T* __restrict__ Bt, int64_t ld, int64_t nbb, int64_t ms, T* __restrict__ Vt) {
+  const int64_t total = nbb * ms;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = e / ms, i = e - j * ms;
+    Vt[e] = (i < j) ? zero_<T>() : (i == j ? one_<T>() : Bt[j * ld + i]);
+  }
+}
+
+// T of a panel (nbb x nbb, upper triangular) from S = V^H V and tau, column by
+// column: T[j][j] = tau_j, T[0:j, j] = T[0:j, 0:j] (-tau_j S[0:j, j]).  One CTA
+// of kQrNB threads, thread i owns row i; T and column j of S are staged in
+// shared memory (dynamic, nbb * nbb + nbb elements).
+template <typename T>
+__global__ void qr_form_t(const T* __restrict__ S, const T* __restrict__ tau, int64_t nbb, T* __restrict__ Tm) {
+  extern __shared__ __align__(16) unsigned char qr_t_smem[];
+  T* sT = reinterpret_cast<T*>(qr_t_smem);
+  T* sy = sT + nbb * nbb;
+  const int64_t i = threadIdx.x;
+  for (int64_t e = i; e < nbb * nbb; e += blockDim.x) sT[e] = zero_<T>();
+  __syncthreads();
+  for (int64_t j = 0; j < nbb; ++j) {
+    const T tj = tau[j];
+    if (i < j) sy[i] = -(tj * S[i * nbb + j]);
+    __syncthreads();
+    if (i < j) {
+      T acc0 = zero_<T>(), acc1 = zero_<T>();
+      int64_t l = i;
+      for (; l + 1 < j; l += 2) {
+        acc0 += sT[i * nbb + l] * sy[l];
+        acc1 += sT[i * nbb + l + 1] * sy[l + 1];
+      }
+      if (l < j) acc0 += sT[i * nbb + l] * sy[l];
+      sT[i * nbb + j] = acc0 + acc1;
+    } else if (i == j) {
+      sT[i * nbb + j] = tj;
+    }
+    __syncthreads();
+  }
+  for (int64_t e = i; e < nbb * nbb; e += blockDim.x) Tm[e] = sT[e];
+}
+
+// Dynamic shared memory of qr_form_t beyond the 48 KB default (complex128):
+// raised once per device.
+template <typename T>
+static int ensure_form_t_smem() {
+  constexpr size_t bytes = (size_t)(kQrNB * kQrNB + kQrNB) * sizeof(T);
+  if constexpr (bytes <= 48 * 1024) {
+    return TNC_OK;
+  } else {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TNC_ERR_CUDA;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load() & bit) return TNC_OK;
+    if (cudaFuncSetAttribute((const void*)qr_form_t<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess)
+      return TNC_ERR_CUDA;
+    done.fetch_or(bit);
+    return TNC_OK;
+  }
+}
+
+// C (rows x cols, ld ldc) = sum over nparts of P[p] (rows x cols, dense)
+template <typename T>
+__global__ void qr_sum_parts(const T* __restrict__ P, int64_t nparts, int64_t rows, int64_t cols, T* __restrict__ C,
+                             int64_t ldc) {
+  const int64_t total = rows * cols;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    T acc = zero_<T>();
+    for (int64_t p = 0; p < nparts; ++p) acc += P[p * total + e];
+    const int64_t r = e / cols, c = e - r * cols;
+    C[r * ldc + c] = acc;
+  }
+}
+
+// Qt = the first k rows of the m x m identity
+template <typename T>
+__global__ void qr_eye_rows(T* Qt, int64_t k, int64_t m) {
+  const int64_t total = k * m;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = e / m, i = e - j * m;
+    Qt[e] = (i == j) ? one_<T>() : zero_<T>();
+  }
+}
+
+// C = alpha op(A) op(B) + beta C: tensor cores for FP32-class types when the
+// product is large enough and the workspace holds its split operands
+template <typename T>
+static int qr_gemm(int opA, int opB, int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, const T* B,
+                   int64_t ldb, T beta, T* C, int64_t ldc, void* tcws, size_t tcwb, cudaStream_t st) {
+  if constexpr (sizeof(typename traits<T>::real) == 4) {
+    if (tcws != nullptr && M >= 64 && N >= 64 && K >= 32 && (double)M * N * K >= (double)(1 << 21)) {
+      size_t need = 0;
+      if (tnc_gemm_tc_workspace_size(dtype_of<T>(), M, N, K, 1, &need) == TNC_OK && need <= tcwb) {
+        double a[2], b[2];
+        if constexpr (traits<T>::is_complex) { a[0] = alpha.re; a[1] = alpha.im; b[0] = beta.re; b[1] = beta.im; }
+        else { a[0] = alpha; a[1] = 0; b[0] = beta; b[1] = 0; }
+        return tnc_gemm_tc(dtype_of<T>(), opA, opB, M, N, K, a, A, lda, 0, B, ldb, 0, b, C, ldc, 0, 1, tcws, tcwb,
+                           st);
+      }
+    }
+  }
+  return gemm_launch<T>(opA, opB, M, N, K, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
+}
+
+// C (M x N, ld ldc) = op(A) op(B) with A (M x K, row-major, opA N or R) and B
+// (N x K, row-major, opB T or C): the K range is cut into chunks of kQrSplitK,
+// each chunk one member of a batched CUDA-core GEMM into P, then the partial
+// products are summed -- enough CTAs for the long-K, narrow products of the
+// blocked QR, at FP32 accuracy.
+template <typename T>
+static int qr_gemm_splitk(int opA, int opB, int64_t M, int64_t N, int64_t K, const T* A, int64_t lda, const T* B,
+                          int64_t ldb, T* C, int64_t ldc, T* P, cudaStream_t st) {
+  const int64_t nparts = (K + kQrSplitK - 1) / kQrSplitK;
+  const int64_t full = K / kQrSplitK;  // chunks of full length
+  const T one = one_<T>(), zero = zero_<T>();
+  if (full > 0) {
+    if (int rc = gemm_launch<T>(opA, opB, M, N, kQrSplitK, one, A, lda, kQrSplitK, B, ldb, kQrSplitK, zero, P, N, M * N,
+                                full, st))
+      return rc;
+  }
+  if (full < nparts) {  // the ragged last chunk
+    const int64_t k0 = full * kQrSplitK;
+    if (int rc = gemm_launch<T>(opA, opB, M, N, K - k0, one, A + k0, lda, 0, B + k0, ldb, 0, zero, P + full * M * N, N,
+                                0, 1, st))
+      return rc;
+  }
+  qr_sum_parts<T><<<grid1d(M * N, 256), 256, 0, st>>>(P, nparts, M, N, C, ldc);
+  return launch_status(1);
+}
+
+// Unblocked dataflow factorisation of the m x n matrix whose transpose is at
+// Bt (row stride ld): reflectors in place, tau, per-column flags (zeroed by
+// the caller), errors in sw.  Returns the register width E of the panel
+// kernel used (0: the general kernel).
+template <typename T>
+static int qr_dataflow(int64_t m, int64_t n, int64_t ld, T* Bt, T* tau, int* flags, SyncWords* sw, cudaStream_t st,
+                       int* E_used) {
+  void* args[] = {(void*)&Bt, (void*)&m, (void*)&n, (void*)&ld, (void*)&tau, (void*)&flags, (void*)&sw};
+  // register-resident panels when the column fits (E slots of 32 rows)
+  const void* panel_fn = nullptr;
+  int E = 0;
+  const int64_t slots = (m + 31) / 32;
+  const int64_t maxE = sizeof(T) >= 16 ? 16 : 48;
+  if (slots <= 8) { panel_fn = (const void*)qr_panel_kernel<T, 8>; E = 8; }
+  else if (slots <= 16) { panel_fn = (const void*)qr_panel_kernel<T, 16>; E = 16; }
+  else if constexpr (sizeof(T) < 16) {
+    if (slots <= 32 && maxE >= 32) { panel_fn = (const void*)qr_panel_kernel<T, 32>; E = 32; }
+    else if (slots <= 48 && maxE >= 48) { panel_fn = (const void*)qr_panel_kernel<T, 48>; E = 48; }
+  }
+  if (panel_fn != nullptr) {
+    const int64_t want = (n + kPanel - 1) / kPanel;
+    const int cap = coop_capacity(panel_fn, kPanel * 32, 0);
+    if (cap > 0 && want <= cap) {
+      if (cudaLaunchCooperativeKernel(panel_fn, dim3((unsigned)want), dim3(kPanel * 32), args, 0, st) != cudaSuccess)
+        return TNC_ERR_CUDA;
+      *E_used = E;
+      return launch_status(1);
+    }
+  }
+  *E_used = 0;
+  const int threads = kQrWarps * 32;
+  int cap = coop_capacity((const void*)qr_factor_kernel<T>, threads, 0);
+  if (cap <= 0) return TNC_ERR_CUDA;
+  int64_t want = (n + kQrWarps - 1) / kQrWarps;
+  int grid = (int)(want < cap ? want : cap);
+  if (cudaLaunchCooperativeKernel((const void*)qr_factor_kernel<T>, dim3(grid), dim3(threads), args, 0, st) !=
+      cudaSuccess)
+    return TNC_ERR_CUDA;
+  return launch_status(1);
 }
 
 // Householder factorisation of the m x n matrix X whose transpose is already
@@ -359,59 +575,99 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
   int* flags = (int*)(w + L.flags);
   SyncWords* sw = (SyncWords*)(w + L.sync);
   T* Qt = (T*)(w + L.qt);
+  const bool form_q = (Q != nullptr || want_qt);
   if (cudaMemsetAsync(flags, 0, (size_t)k * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(info, 0, sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
-  int64_t mm = m, nn = n;
-  void* args[] = {(void*)&Bt, (void*)&mm, (void*)&nn, (void*)&tau, (void*)&flags, (void*)&sw};
-  // register-resident panels when the column fits (E slots of 32 rows)
-  const void* panel_fn = nullptr;
-  void (*formq_fn)(const T*, int64_t, int64_t, const T*, T*) = nullptr;
-  const int64_t slots = (m + 31) / 32;
-  const int64_t maxE = sizeof(T) >= 16 ? 16 : 48;
-  if (slots <= 8) { panel_fn = (const void*)qr_panel_kernel<T, 8>; formq_fn = qr_form_q_reg_kernel<T, 8>; }
-  else if (slots <= 16) { panel_fn = (const void*)qr_panel_kernel<T, 16>; formq_fn = qr_form_q_reg_kernel<T, 16>; }
-  else if constexpr (sizeof(T) < 16) {
-    if (slots <= 32 && maxE >= 32) { panel_fn = (const void*)qr_panel_kernel<T, 32>; formq_fn = qr_form_q_reg_kernel<T, 32>; }
-    else if (slots <= 48 && maxE >= 48) { panel_fn = (const void*)qr_panel_kernel<T, 48>; formq_fn = qr_form_q_reg_kernel<T, 48>; }
-  }
-  bool used_panel = false;
-  if (panel_fn != nullptr) {
-    const int64_t want = (n + kPanel - 1) / kPanel;
-    const int cap = coop_capacity(panel_fn, kPanel * 32, 0);
-    if (cap > 0 && want <= cap) {
-      if (cudaLaunchCooperativeKernel(panel_fn, dim3((unsigned)want), dim3(kPanel * 32), args, 0, st) != cudaSuccess)
-        return TNC_ERR_CUDA;
-      used_panel = true;
+  if (!L.blocked) {
+    int E = 0;
+    if (int rc = qr_dataflow<T>(m, n, m, Bt, tau, flags, sw, st, &E)) return rc;
+    copy_sync_error<<<1, 1, 0, st>>>(sw, info);
+    int launches = 2;  // error copy, extract R
+    if (form_q) {
+      void (*formq_fn)(const T*, int64_t, int64_t, const T*, T*) = nullptr;
+      if (E == 8) formq_fn = qr_form_q_reg_kernel<T, 8>;
+      else if (E == 16) formq_fn = qr_form_q_reg_kernel<T, 16>;
+      else if constexpr (sizeof(T) < 16) {
+        if (E == 32) formq_fn = qr_form_q_reg_kernel<T, 32>;
+        else if (E == 48) formq_fn = qr_form_q_reg_kernel<T, 48>;
+      }
+      if (formq_fn != nullptr) {
+        int64_t gq = (k + kPanel - 1) / kPanel;
+        formq_fn<<<(unsigned)gq, kPanel * 32, 0, st>>>(Bt, m, k, tau, Qt);
+      } else {
+        const int threads = kQrWarps * 32;
+        int64_t gq = (k + kQrWarps - 1) / kQrWarps;
+        if (gq > 152 * 16) gq = 152 * 16;
+        qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
+      }
+      ++launches;
+    }
+    qr_extract_r<T><<<grid1d(k * n, 256), 256, 0, st>>>(Bt, m, n, k, R);
+    if (launch_status(launches)) return TNC_ERR_CUDA;
+  } else {
+    T* Vt = (T*)(w + L.vt);
+    T* S = (T*)(w + L.s);
+    T* Tall = (T*)(w + L.tm);
+    T* Wt = (T*)(w + L.wt);
+    T* W2t = (T*)(w + L.w2t);
+    T* P = (T*)(w + L.part);
+    void* tcws = L.tcws_bytes ? (void*)(w + L.tcws) : nullptr;
+    const T one = one_<T>(), zero = zero_<T>(), mone = zero_<T>() - one_<T>();
+    const int64_t nblk = (k + kQrNB - 1) / kQrNB;
+    if (int rc = ensure_form_t_smem<T>()) return rc;
+    for (int64_t b = 0; b < nblk; ++b) {
+      const int64_t c0 = b * kQrNB;
+      const int64_t nbb = (k - c0) < kQrNB ? (k - c0) : kQrNB;
+      const int64_t ms = m - c0;
+      T* panel = Bt + c0 * m + c0;
+      int E = 0;
+      if (int rc = qr_dataflow<T>(ms, nbb, m, panel, tau + c0, flags + c0, sw, st, &E)) return rc;
+      const int64_t n2 = n - c0 - nbb;
+      const bool need_t = form_q || n2 > 0;
+      if (!need_t) continue;
+      qr_extract_vt<T><<<grid1d(nbb * ms, 256), 256, 0, st>>>(panel, m, nbb, ms, Vt);
+      // S = V^H V = conj(Vt) Vt^T
+      if (int rc = qr_gemm_splitk<T>(TNC_OP_R, TNC_OP_T, nbb, nbb, ms, Vt, ms, Vt, ms, S, nbb, P, st)) return rc;
+      T* Tb = Tall + b * kQrNB * kQrNB;
+      qr_form_t<T><<<1, kQrNB, (size_t)(nbb * nbb + nbb) * sizeof(T), st>>>(S, tau + c0, nbb, Tb);
+      if (launch_status(2)) return TNC_ERR_CUDA;
+      if (n2 > 0) {
+        T* X2t = Bt + (c0 + nbb) * m + c0;  // trailing columns, rows c0.. (n2 x ms, ld m)
+        if (int rc = qr_gemm_splitk<T>(TNC_OP_N, TNC_OP_C, n2, nbb, ms, X2t, m, Vt, ms, Wt, nbb, P, st)) return rc;
+        // W2t = Wt conj(T)   (W2 = T^H W)
+        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_R, n2, nbb, nbb, one, Wt, nbb, Tb, nbb, zero, W2t, nbb, nullptr, 0, st))
+          return rc;
+        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_N, n2, ms, nbb, mone, W2t, nbb, Vt, ms, one, X2t, m, tcws,
+                                L.tcws_bytes, st))
+          return rc;
+      }
+    }
+    copy_sync_error<<<1, 1, 0, st>>>(sw, info);
+    qr_extract_r<T><<<grid1d(k * n, 256), 256, 0, st>>>(Bt, m, n, k, R);
+    if (launch_status(2)) return TNC_ERR_CUDA;
+    if (form_q) {
+      qr_eye_rows<T><<<grid1d(k * m, 256), 256, 0, st>>>(Qt, k, m);
+      if (launch_status(1)) return TNC_ERR_CUDA;
+      for (int64_t b = nblk - 1; b >= 0; --b) {
+        const int64_t c0 = b * kQrNB;
+        const int64_t nbb = (k - c0) < kQrNB ? (k - c0) : kQrNB;
+        const int64_t ms = m - c0;
+        const int64_t nq = k - c0;            // columns of Q touched
+        T* Qs = Qt + c0 * m + c0;             // nq x ms, ld m
+        const T* Tb = Tall + b * kQrNB * kQrNB;
+        qr_extract_vt<T><<<grid1d(nbb * ms, 256), 256, 0, st>>>(Bt + c0 * m + c0, m, nbb, ms, Vt);
+        if (launch_status(1)) return TNC_ERR_CUDA;
+        if (int rc = qr_gemm_splitk<T>(TNC_OP_N, TNC_OP_C, nq, nbb, ms, Qs, m, Vt, ms, Wt, nbb, P, st)) return rc;
+        // W2t = Wt T^T   (W2 = T W)
+        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_T, nq, nbb, nbb, one, Wt, nbb, Tb, nbb, zero, W2t, nbb, nullptr, 0, st))
+          return rc;
+        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_N, nq, ms, nbb, mone, W2t, nbb, Vt, ms, one, Qs, m, tcws,
+                                L.tcws_bytes, st))
+          return rc;
+      }
     }
   }
-  if (!used_panel) {
-    formq_fn = nullptr;
-    const int threads = kQrWarps * 32;
-    int cap = coop_capacity((const void*)qr_factor_kernel<T>, threads, 0);
-    if (cap <= 0) return TNC_ERR_CUDA;
-    int64_t want = (n + kQrWarps - 1) / kQrWarps;
-    int grid = (int)(want < cap ? want : cap);
-    if (cudaLaunchCooperativeKernel((const void*)qr_factor_kernel<T>, dim3(grid), dim3(threads), args, 0, st) !=
-        cudaSuccess)
-      return TNC_ERR_CUDA;
-  }
-  copy_sync_error<<<1, 1, 0, st>>>(sw, info);
-  int launches = 3;  // factor, error copy, extract R
-  if (Q != nullptr || want_qt) {
-    if (formq_fn != nullptr) {
-      int64_t gq = (k + kPanel - 1) / kPanel;
-      formq_fn<<<(unsigned)gq, kPanel * 32, 0, st>>>(Bt, m, k, tau, Qt);
-    } else {
-      const int threads = kQrWarps * 32;
-      int64_t gq = (k + kQrWarps - 1) / kQrWarps;
-      if (gq > 152 * 16) gq = 152 * 16;
-      qr_form_q_kernel<T><<<(unsigned)gq, threads, 0, st>>>(Bt, m, k, tau, Qt);
-    }
-    ++launches;
-  }
-  qr_extract_r<T><<<grid1d(k * n, 256), 256, 0, st>>>(Bt, m, n, k, R);
-  if (launch_status(launches)) return TNC_ERR_CUDA;
   if (Q == nullptr) return TNC_OK;
   // Q = Qt^T
   int64_t shp[2] = {k, m};
@@ -424,7 +680,7 @@ static int qr_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* Q, T* R, vo
                    int* info, cudaStream_t st) {
   if (m <= 0 || n <= 0 || lda < n || !A || !Q || !R || !work || !info) return TNC_ERR_ARG;
   if (lda != n) return TNC_ERR_ARG;
-  QrLayout L = qr_layout(m, n, sizeof(T));
+  QrLayout L = qr_layout(m, n, dtype_of<T>());
   if (wb < L.total) return TNC_ERR_WORKSPACE;
   char* w = (char*)work;
   // Bt = A^T
@@ -442,7 +698,7 @@ static int qr_r_impl(int64_t m, int64_t n, const T* A, int adjoint, T* R, void* 
                      cudaStream_t st) {
   if (m <= 0 || n <= 0 || !A || !R || !work || !info) return TNC_ERR_ARG;
   const int64_t fm = adjoint ? n : m, fn = adjoint ? m : n;  // the factorised matrix is fm x fn
-  QrLayout L = qr_layout(fm, fn, sizeof(T));
+  QrLayout L = qr_layout(fm, fn, dtype_of<T>());
   if (wb < L.total) return TNC_ERR_WORKSPACE;
   char* w = (char*)work;
   if (adjoint) {
@@ -462,13 +718,13 @@ static int qr_r_impl(int64_t m, int64_t n, const T* A, int adjoint, T* R, void* 
 
 namespace tnc {
 
-size_t qr_qt_workspace(int64_t fm, int64_t fn, size_t es) { return qr_layout(fm, fn, es).total; }
+size_t qr_qt_workspace(int64_t fm, int64_t fn, int dt) { return qr_layout(fm, fn, dt).total; }
 
 template <typename T>
 int qr_qt(int64_t fm, int64_t fn, const T* A, int adjoint, bool want_qt, T* R, void* work, size_t wb, int* info,
           cudaStream_t st, T** qt) {
   if (fm <= 0 || fn <= 0 || !A || !R || !work || !info) return TNC_ERR_ARG;
-  QrLayout L = qr_layout(fm, fn, sizeof(T));
+  QrLayout L = qr_layout(fm, fn, dtype_of<T>());
   if (wb < L.total) return TNC_ERR_WORKSPACE;
   char* w = (char*)work;
   // Bt = X^T: for X = A^H that is conj(A) as stored (A is fn x fm)
@@ -492,9 +748,8 @@ template int qr_qt<c128>(int64_t, int64_t, const c128*, int, bool, c128*, void*,
 using namespace tnc;
 
 extern "C" int tnc_qr_workspace_size(int dtype, int64_t m, int64_t n, size_t* bytes) {
-  int es = elem_size(dtype);
-  if (!es || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
-  *bytes = qr_layout(m, n, es).total;
+  if (!elem_size(dtype) || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
+  *bytes = qr_layout(m, n, dtype).total;
   return TNC_OK;
 }
 
@@ -506,9 +761,8 @@ extern "C" int tnc_qr(int dtype, int64_t m, int64_t n, const void* A, int64_t ld
 }
 
 extern "C" int tnc_qr_r_workspace_size(int dtype, int64_t m, int64_t n, int adjoint, size_t* bytes) {
-  int es = elem_size(dtype);
-  if (!es || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
-  *bytes = adjoint ? qr_layout(n, m, es).total : qr_layout(m, n, es).total;
+  if (!elem_size(dtype) || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
+  *bytes = adjoint ? qr_layout(n, m, dtype).total : qr_layout(m, n, dtype).total;
   return TNC_OK;
 }
 

@@ -164,11 +164,11 @@ struct SvdLayout {
 static const int kMaxSweepsCap = 100;
 // [QR workspace of X (L x nr): its transposed copy, reused for the small
 //  output factor once R is out; tau; flags; Q^T] [W = R, nr x nr] [J] ...
-static SvdLayout svd_layout(int64_t m, int64_t n, size_t es, size_t rs) {
+static SvdLayout svd_layout(int64_t m, int64_t n, int dt, size_t es, size_t rs) {
   int64_t nr = m < n ? m : n, L = m < n ? n : m;
   SvdLayout Ly;
   size_t off = 0;
-  Ly.qr = off; off = align256(off + qr_qt_workspace(L, nr, es));
+  Ly.qr = off; off = align256(off + qr_qt_workspace(L, nr, dt));
   Ly.w = off; off = align256(off + (size_t)nr * nr * es);
   Ly.j = off; off = align256(off + (size_t)nr * nr * es);
   Ly.d = off; off = align256(off + (size_t)nr * rs);
@@ -202,7 +202,7 @@ static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typenam
                     int max_sweeps, double tol, void* work, size_t wb, int* info, cudaStream_t st) {
   typedef typename traits<T>::real R;
   if (m <= 0 || n <= 0 || lda != n || !A || !U || !S || !VH || !work || !info) return TNC_ERR_ARG;
-  SvdLayout Ly = svd_layout(m, n, sizeof(T), sizeof(R));
+  SvdLayout Ly = svd_layout(m, n, dtype_of<T>(), sizeof(T), sizeof(R));
   if (wb < Ly.total) return TNC_ERR_WORKSPACE;
   if (max_sweeps <= 0) max_sweeps = 40;
   if (max_sweeps > kMaxSweepsCap) max_sweeps = kMaxSweepsCap;
@@ -222,7 +222,7 @@ static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typenam
   double* frob2 = (double*)(w + Ly.frob2);
   T* Qt = nullptr;
   // X = A^H (wide) or A (tall); R of X into W, Q^T (nr x L) kept in the QR workspace
-  int s = qr_qt<T>(L, nr, A, tall ? 0 : 1, true, W, w + Ly.qr, qr_qt_workspace(L, nr, sizeof(T)), info, st, &Qt);
+  int s = qr_qt<T>(L, nr, A, tall ? 0 : 1, true, W, w + Ly.qr, qr_qt_workspace(L, nr, dtype_of<T>()), info, st, &Qt);
   if (s) return s;
   T* small = (T*)(w + Ly.qr);  // the QR's transposed copy (nr * L >= nr * nr elements) is free now
   eye_kernel<T><<<grid1d(nr * nr, 256), 256, 0, st>>>(J, nr);
@@ -271,7 +271,7 @@ extern "C" int tnc_svd_workspace_size(int dtype, int64_t m, int64_t n, size_t* b
   int es = elem_size(dtype);
   if (!es || m <= 0 || n <= 0 || !bytes) return TNC_ERR_ARG;
   size_t rs = (dtype == TNC_F32 || dtype == TNC_C64) ? 4 : 8;
-  *bytes = svd_layout(m, n, es, rs).total;
+  *bytes = svd_layout(m, n, dtype, es, rs).total;
   return TNC_OK;
 }
 
