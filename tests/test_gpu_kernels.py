@@ -126,6 +126,23 @@ def test_qr_r_only(gpu, dt, shape):
         assert relerr(np.conj(R).T @ R, np.conj(X).T @ X) < t
 
 
+@pytest.mark.parametrize("dt", DTYPES)
+def test_qr_blocked_degenerate(gpu, dt):
+    """Blocked QR (k >= 128) with a column already in triangular form (its
+    reflector is the identity, tau = 0), a zero column and a repeated column."""
+    from tncontract_gb300 import _ops
+    rng = np.random.default_rng(15)
+    A = rnd(rng, (300, 200), dt)
+    A[:, 0] = 0
+    A[0, 0] = 2
+    A[:, 70] = 0
+    A[:, 150] = A[:, 5]
+    Q, R = (host(x) for x in _ops.qr(dev(A)))
+    t = tol(dt) * 300
+    assert relerr(Q @ R, A) < t
+    assert np.linalg.norm(np.conj(Q).T @ Q - np.eye(200)) < t * np.sqrt(200)
+
+
 def test_qr_rank_deficient(gpu):
     from tncontract_gb300 import _ops
     rng = np.random.default_rng(5)

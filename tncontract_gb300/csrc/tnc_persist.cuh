@@ -5,6 +5,8 @@
 #pragma once
 #include "tnc_common.cuh"
 
+#include <mutex>
+
 namespace tnc {
 
 // Roughly 2-4 s of polling at ~150 ns per iteration: orders of magnitude above
@@ -216,14 +218,30 @@ __device__ __forceinline__ typename traits<T>::real noise_floor2(const double* f
   return (typename traits<T>::real)(traits<T>::eps * traits<T>::eps * f2[0]);
 }
 
-// Largest co-resident grid for a cooperative launch of `kernel`.
+// Largest co-resident grid for a cooperative launch of `kernel`; the answer
+// is cached per (device, kernel, block size, shared memory), the occupancy
+// query being host work on the launch path of every call.
 inline int coop_capacity(const void* kernel, int threads, size_t smem) {
-  int dev = 0, sms = 0, per = 0, coop = 0;
+  struct Entry { const void* k; int threads, dev; size_t smem; int cap; };
+  static Entry cache[256];
+  static int used = 0;
+  static std::mutex mu;
+  int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < used; ++i)
+      if (cache[i].k == kernel && cache[i].threads == threads && cache[i].smem == smem && cache[i].dev == dev)
+        return cache[i].cap;
+  }
+  int sms = 0, per = 0, coop = 0;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess) return 0;
-  return per * sms;
+  const int cap = per * sms;
+  std::lock_guard<std::mutex> lock(mu);
+  if (used < 256) cache[used++] = Entry{kernel, threads, dev, smem, cap};
+  return cap;
 }
 
 }  // namespace tnc

@@ -172,18 +172,20 @@ __device__ __forceinline__ T reg_get(const T (&x)[E], int64_t i) {
   return shfl_T(a, (int)(i & 31));
 }
 
-// larfg on the register column: entries > c scaled to v, entry c = beta
+// larfg on the register column: entries > c scaled to v, entry c = beta.
+// Norm with four independent partial sums (short dependency chains).
 template <typename T, int E>
 __device__ __forceinline__ T make_reflector_reg(T (&x)[E], int64_t c, int64_t m) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
-  R xn = 0;
+  R xn0 = 0, xn1 = 0, xn2 = 0, xn3 = 0;
 #pragma unroll
   for (int u = 0; u < E; ++u) {
     const int64_t i = lane + 32 * u;
-    if (i > c && i < m) xn += abs2_(x[u]);
+    const R a = (i > c && i < m) ? abs2_(x[u]) : R(0);
+    if ((u & 3) == 0) xn0 += a; else if ((u & 3) == 1) xn1 += a; else if ((u & 3) == 2) xn2 += a; else xn3 += a;
   }
-  xn = warp_sum(xn);
+  const R xn = warp_sum((xn0 + xn1) + (xn2 + xn3));
   const T alpha = reg_get(x, c);
   T tau = zero_<T>();
   if (!(xn == R(0) && imag_(alpha) == R(0))) {
@@ -201,18 +203,71 @@ __device__ __forceinline__ T make_reflector_reg(T (&x)[E], int64_t c, int64_t m)
   return tau;
 }
 
-// x <- H_c^H x with v held in registers vv (v_c = 1 implied)
+// x <- H_c^H x, v read twice from `v` (entries i > c; v_c = 1 implied):
+// shared memory for the panel's own reflectors, L2 for earlier panels'.  Each
+// pass fetches v in chunks of C independent loads before using them (keeps
+// the L2 latency overlapped without a full register copy of v); the dot
+// product runs four independent partial sums.
+template <typename T, int E, bool GLOBAL>
+__device__ __forceinline__ void apply_stream(T (&x)[E], const T* v, T tau, int64_t c, int64_t m) {
+  constexpr int C = (E % 16 == 0 && E < 48) ? 16 : 8;
+  const int lane = threadIdx.x & 31;
+  T w0 = zero_<T>(), w1 = zero_<T>(), w2 = zero_<T>(), w3 = zero_<T>();
+#pragma unroll
+  for (int u0 = 0; u0 < E; u0 += C) {
+    T vc[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int64_t i = lane + 32 * (u0 + q);
+      vc[q] = (i > c && i < m) ? (GLOBAL ? ldcg(v + i) : v[i]) : zero_<T>();
+    }
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int u = u0 + q;
+      const int64_t i = lane + 32 * u;
+      if (i == c) w0 += x[u];
+      else if ((q & 3) == 0) fma_(w0, conj_(vc[q]), x[u]);
+      else if ((q & 3) == 1) fma_(w1, conj_(vc[q]), x[u]);
+      else if ((q & 3) == 2) fma_(w2, conj_(vc[q]), x[u]);
+      else fma_(w3, conj_(vc[q]), x[u]);
+    }
+  }
+  const T w = warp_sum((w0 + w1) + (w2 + w3));
+  const T f = conj_(tau) * w;
+#pragma unroll
+  for (int u0 = 0; u0 < E; u0 += C) {
+    T vc[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int64_t i = lane + 32 * (u0 + q);
+      vc[q] = (i > c && i < m) ? (GLOBAL ? ldcg(v + i) : v[i]) : zero_<T>();
+    }
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int u = u0 + q;
+      const int64_t i = lane + 32 * u;
+      if (i == c) x[u] = x[u] - f;
+      else x[u] = x[u] - f * vc[q];  // vc is 0 outside (c, m)
+    }
+  }
+}
+
+// x <- H_c^H x with v held in registers vv (v_c = 1 implied); used by the
+// Q formation kernel below
 template <typename T, int E>
 __device__ __forceinline__ void apply_reg(T (&x)[E], const T (&vv)[E], T tau, int64_t c, int64_t m) {
   const int lane = threadIdx.x & 31;
-  T w = zero_<T>();
+  T w0 = zero_<T>(), w1 = zero_<T>();
 #pragma unroll
   for (int u = 0; u < E; ++u) {
     const int64_t i = lane + 32 * u;
-    if (i == c) w += x[u];
-    else if (i > c && i < m) fma_(w, conj_(vv[u]), x[u]);
+    if (i == c) w0 += x[u];
+    else if (i > c && i < m) {
+      if (u & 1) fma_(w1, conj_(vv[u]), x[u]);
+      else fma_(w0, conj_(vv[u]), x[u]);
+    }
   }
-  w = warp_sum(w);
+  const T w = warp_sum(w0 + w1);
   const T f = conj_(tau) * w;
 #pragma unroll
   for (int u = 0; u < E; ++u) {
@@ -225,15 +280,14 @@ __device__ __forceinline__ void apply_reg(T (&x)[E], const T (&vv)[E], T tau, in
 template <typename T, int E>
 __global__ void __launch_bounds__(kPanel * 32)
 qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, SyncWords* sw) {
-  __shared__ T sv[32 * E];
-  __shared__ T stau;
+  __shared__ T sv[2 * 32 * E];
+  __shared__ T stau[2];
   const int64_t k = m < n ? m : n;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t p0 = (int64_t)blockIdx.x * kPanel;  // first column of the panel
   const int64_t j = p0 + warp;                      // my column
   const bool has = j < n;
   T x[E];
-  T vv[E];
   if (has) {
 #pragma unroll
     for (int u = 0; u < E; ++u) {
@@ -241,53 +295,58 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
       x[u] = (i < m) ? Bt[j * ld + i] : zero_<T>();
     }
   }
-  // reflectors of earlier panels, as they are published
+  // reflectors of earlier panels, as they are published (read from L2)
   const int64_t cend = p0 < k ? p0 : k;
   if (has) {
     for (int64_t c = 0; c < cend; ++c) {
       if (!warp_wait_flag(&flags[c], sw)) break;
-#pragma unroll
-      for (int u = 0; u < E; ++u) {
-        const int64_t i = lane + 32 * u;
-        vv[u] = (i > c && i < m) ? ldcg(Bt + c * ld + i) : zero_<T>();
-      }
-      apply_reg(x, vv, ldcg(tau + c), c, m);
+      apply_stream<T, E, true>(x, Bt + c * ld, ldcg(tau + c), c, m);
     }
   }
   __syncthreads();
   if (ld_volatile(&sw->err)) return;  // uniform: every warp sees the same error word after the barrier
-  // this panel's reflectors
-  for (int w = 0; w < kPanel; ++w) {
+  // this panel's reflectors.  Reflector c is written to shared memory buffer
+  // (c & 1) by its owner; after one CTA barrier the later columns apply it
+  // while the owner publishes it to global memory, and the owner of column
+  // c+1 builds reflector c+1 into the other buffer right after applying c
+  // (look-ahead), so each column costs one barrier.
+  const int64_t nw = (k - p0) < kPanel ? (k - p0) : kPanel;
+  if (nw > 0 && warp == 0) {
+    const T t = make_reflector_reg(x, p0, m);
+#pragma unroll
+    for (int u = 0; u < E; ++u) {
+      const int64_t i = lane + 32 * u;
+      if (i < m) sv[i] = x[u];
+    }
+    if (lane == 0) stau[0] = t;
+  }
+  for (int w = 0; w < nw; ++w) {
     const int64_t c = p0 + w;
-    if (c >= k) break;  // uniform over the CTA
+    const int b = w & 1;
+    __syncthreads();
     if (warp == w) {
-      const T t = make_reflector_reg(x, c, m);
 #pragma unroll
       for (int u = 0; u < E; ++u) {
         const int64_t i = lane + 32 * u;
-        if (i < m) {
-          sv[i] = x[u];
-          if (i >= c) stcg(Bt + c * ld + i, x[u]);
-        }
+        if (i >= c && i < m) stcg(Bt + c * ld + i, x[u]);
       }
-      if (lane == 0) {
-        stau = t;
-        stcg(tau + c, t);
-      }
+      if (lane == 0) stcg(tau + c, stau[b]);
       __threadfence();
       __syncwarp();
       if (lane == 0) atomicExch(&flags[c], 1);
-    }
-    __syncthreads();
-    if (has && warp > w) {
+    } else if (has && warp > w) {
+      apply_stream<T, E, false>(x, sv + b * (32 * E), stau[b], c, m);
+      if (warp == w + 1 && w + 1 < nw) {
+        const T t = make_reflector_reg(x, c + 1, m);
+        T* nb = sv + (b ^ 1) * (32 * E);
 #pragma unroll
-      for (int u = 0; u < E; ++u) {
-        const int64_t i = lane + 32 * u;
-        vv[u] = (i > c && i < m) ? sv[i] : zero_<T>();
+        for (int u = 0; u < E; ++u) {
+          const int64_t i = lane + 32 * u;
+          if (i < m) nb[i] = x[u];
+        }
+        if (lane == 0) stau[b ^ 1] = t;
       }
-      apply_reg(x, vv, stau, c, m);
     }
-    __syncthreads();
   }
   if (has) {
 #pragma unroll
@@ -398,41 +457,64 @@ __global__ void qr_extract_vt(const T* __restrict__ Bt, int64_t ld, int64_t nbb,
   }
 }
 
-// T of a panel (nbb x nbb, upper triangular) from S = V^H V and tau, column by
-// column: T[j][j] = tau_j, T[0:j, j] = T[0:j, 0:j] (-tau_j S[0:j, j]).  One CTA
-// of kQrNB threads, thread i owns row i; T and column j of S are staged in
-// shared memory (dynamic, nbb * nbb + nbb elements).
-template <typename T>
-__global__ void qr_form_t(const T* __restrict__ S, const T* __restrict__ tau, int64_t nbb, T* __restrict__ Tm) {
-  extern __shared__ __align__(16) unsigned char qr_t_smem[];
-  T* sT = reinterpret_cast<T*>(qr_t_smem);
-  T* sy = sT + nbb * nbb;
-  const int64_t i = threadIdx.x;
-  for (int64_t e = i; e < nbb * nbb; e += blockDim.x) sT[e] = zero_<T>();
-  __syncthreads();
-  for (int64_t j = 0; j < nbb; ++j) {
-    const T tj = tau[j];
-    if (i < j) sy[i] = -(tj * S[i * nbb + j]);
-    __syncthreads();
-    if (i < j) {
-      T acc0 = zero_<T>(), acc1 = zero_<T>();
-      int64_t l = i;
-      for (; l + 1 < j; l += 2) {
-        acc0 += sT[i * nbb + l] * sy[l];
-        acc1 += sT[i * nbb + l + 1] * sy[l + 1];
-      }
-      if (l < j) acc0 += sT[i * nbb + l] * sy[l];
-      sT[i * nbb + j] = acc0 + acc1;
-    } else if (i == j) {
-      sT[i * nbb + j] = tj;
-    }
-    __syncthreads();
-  }
-  for (int64_t e = i; e < nbb * nbb; e += blockDim.x) Tm[e] = sT[e];
+template <typename T> __device__ __forceinline__ bool is_zero_(T v) {
+  if constexpr (traits<T>::is_complex) return v.re == 0 && v.im == 0; else return v == 0;
 }
 
-// Dynamic shared memory of qr_form_t beyond the 48 KB default (complex128):
-// raised once per device.
+// The block reflector's T enters only as T^H W (trailing update) and T W (Q
+// formation).  For Householder blocks T^-1 = U = striu(S) + diag(1/tau) with
+// S = V^H V (from Q = I - V T V^H unitary: T^-1 + T^-H = V^H V, T^-1 upper
+// triangular), so both products are triangular solves against S:
+//   adjoint: U^H W2 = W (forward),   else: U W2 = W (backward).
+// A reflector with tau = 0 (H = I) drops out of the product: its component
+// of W2 is 0 and it is skipped by the others.  Rows of Wt / W2t are columns
+// of W / W2 (rows x nbb); one warp per row, lane l holding components l and
+// l + 32, S and tau staged in shared memory (nbb * nbb + nbb elements).
+template <typename T>
+__global__ void qr_apply_tinv(const T* __restrict__ S, const T* __restrict__ tau, int64_t nbb, const T* __restrict__ Wt,
+                              T* __restrict__ W2t, int64_t rows, int adjoint) {
+  extern __shared__ __align__(16) unsigned char qr_t_smem[];
+  T* sS = reinterpret_cast<T*>(qr_t_smem);
+  T* st = sS + nbb * nbb;
+  for (int64_t e = threadIdx.x; e < nbb * nbb; e += blockDim.x) sS[e] = S[e];
+  for (int64_t e = threadIdx.x; e < nbb; e += blockDim.x) st[e] = tau[e];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int n = (int)nbb;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += nwarps) {
+    const T* wr = Wt + r * nbb;
+    T a0 = zero_<T>(), a1 = zero_<T>();
+    if (adjoint) {
+      for (int i = 0; i < n; ++i) {
+        T p = zero_<T>();
+        if (lane < i) p = conj_(sS[lane * n + i]) * a0;
+        if (lane + 32 < i) p += conj_(sS[(lane + 32) * n + i]) * a1;
+        p = warp_sum(p);
+        const T ti = st[i];
+        const T val = is_zero_(ti) ? zero_<T>() : (wr[i] - p) * conj_(ti);
+        if (lane == i) a0 = val;
+        if (lane + 32 == i) a1 = val;
+      }
+    } else {
+      for (int i = n - 1; i >= 0; --i) {
+        T p = zero_<T>();
+        if (lane > i && lane < n) p = sS[i * n + lane] * a0;
+        if (lane + 32 > i && lane + 32 < n) p += sS[i * n + lane + 32] * a1;
+        p = warp_sum(p);
+        const T ti = st[i];
+        const T val = is_zero_(ti) ? zero_<T>() : (wr[i] - p) * ti;
+        if (lane == i) a0 = val;
+        if (lane + 32 == i) a1 = val;
+      }
+    }
+    if (lane < n) W2t[r * nbb + lane] = a0;
+    if (lane + 32 < n) W2t[r * nbb + lane + 32] = a1;
+  }
+}
+
+// Dynamic shared memory of qr_apply_tinv beyond the 48 KB default
+// (complex128): raised once per device.
 template <typename T>
 static int ensure_form_t_smem() {
   constexpr size_t bytes = (size_t)(kQrNB * kQrNB + kQrNB) * sizeof(T);
@@ -444,7 +526,7 @@ static int ensure_form_t_smem() {
     if (cudaGetDevice(&dev) != cudaSuccess) return TNC_ERR_CUDA;
     const unsigned long long bit = 1ull << (dev & 63);
     if (done.load() & bit) return TNC_OK;
-    if (cudaFuncSetAttribute((const void*)qr_form_t<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+    if (cudaFuncSetAttribute((const void*)qr_apply_tinv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
         cudaSuccess)
       return TNC_ERR_CUDA;
     done.fetch_or(bit);
@@ -607,8 +689,7 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
     if (launch_status(launches)) return TNC_ERR_CUDA;
   } else {
     T* Vt = (T*)(w + L.vt);
-    T* S = (T*)(w + L.s);
-    T* Tall = (T*)(w + L.tm);
+    T* Sall = (T*)(w + L.tm);  // S = V^H V of every panel
     T* Wt = (T*)(w + L.wt);
     T* W2t = (T*)(w + L.w2t);
     T* P = (T*)(w + L.part);
@@ -616,6 +697,7 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
     const T one = one_<T>(), zero = zero_<T>(), mone = zero_<T>() - one_<T>();
     const int64_t nblk = (k + kQrNB - 1) / kQrNB;
     if (int rc = ensure_form_t_smem<T>()) return rc;
+    const size_t tinv_smem = (size_t)(kQrNB * kQrNB + kQrNB) * sizeof(T);
     for (int64_t b = 0; b < nblk; ++b) {
       const int64_t c0 = b * kQrNB;
       const int64_t nbb = (k - c0) < kQrNB ? (k - c0) : kQrNB;
@@ -627,17 +709,16 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
       const bool need_t = form_q || n2 > 0;
       if (!need_t) continue;
       qr_extract_vt<T><<<grid1d(nbb * ms, 256), 256, 0, st>>>(panel, m, nbb, ms, Vt);
-      // S = V^H V = conj(Vt) Vt^T
-      if (int rc = qr_gemm_splitk<T>(TNC_OP_R, TNC_OP_T, nbb, nbb, ms, Vt, ms, Vt, ms, S, nbb, P, st)) return rc;
-      T* Tb = Tall + b * kQrNB * kQrNB;
-      qr_form_t<T><<<1, kQrNB, (size_t)(nbb * nbb + nbb) * sizeof(T), st>>>(S, tau + c0, nbb, Tb);
-      if (launch_status(2)) return TNC_ERR_CUDA;
+      // S = V^H V = conj(Vt) Vt^T, kept per panel for the Q formation
+      T* Sb = Sall + b * kQrNB * kQrNB;
+      if (int rc = qr_gemm_splitk<T>(TNC_OP_R, TNC_OP_T, nbb, nbb, ms, Vt, ms, Vt, ms, Sb, nbb, P, st)) return rc;
+      if (launch_status(1)) return TNC_ERR_CUDA;
       if (n2 > 0) {
         T* X2t = Bt + (c0 + nbb) * m + c0;  // trailing columns, rows c0.. (n2 x ms, ld m)
         if (int rc = qr_gemm_splitk<T>(TNC_OP_N, TNC_OP_C, n2, nbb, ms, X2t, m, Vt, ms, Wt, nbb, P, st)) return rc;
-        // W2t = Wt conj(T)   (W2 = T^H W)
-        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_R, n2, nbb, nbb, one, Wt, nbb, Tb, nbb, zero, W2t, nbb, nullptr, 0, st))
-          return rc;
+        // W2 = T^H W
+        qr_apply_tinv<T><<<grid1d(n2 * 32, 256, 152 * 8), 256, tinv_smem, st>>>(Sb, tau + c0, nbb, Wt, W2t, n2, 1);
+        if (launch_status(1)) return TNC_ERR_CUDA;
         if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_N, n2, ms, nbb, mone, W2t, nbb, Vt, ms, one, X2t, m, tcws,
                                 L.tcws_bytes, st))
           return rc;
@@ -655,13 +736,13 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
         const int64_t ms = m - c0;
         const int64_t nq = k - c0;            // columns of Q touched
         T* Qs = Qt + c0 * m + c0;             // nq x ms, ld m
-        const T* Tb = Tall + b * kQrNB * kQrNB;
+        const T* Sb = Sall + b * kQrNB * kQrNB;
         qr_extract_vt<T><<<grid1d(nbb * ms, 256), 256, 0, st>>>(Bt + c0 * m + c0, m, nbb, ms, Vt);
         if (launch_status(1)) return TNC_ERR_CUDA;
         if (int rc = qr_gemm_splitk<T>(TNC_OP_N, TNC_OP_C, nq, nbb, ms, Qs, m, Vt, ms, Wt, nbb, P, st)) return rc;
-        // W2t = Wt T^T   (W2 = T W)
-        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_T, nq, nbb, nbb, one, Wt, nbb, Tb, nbb, zero, W2t, nbb, nullptr, 0, st))
-          return rc;
+        // W2 = T W
+        qr_apply_tinv<T><<<grid1d(nq * 32, 256, 152 * 8), 256, tinv_smem, st>>>(Sb, tau + c0, nbb, Wt, W2t, nq, 0);
+        if (launch_status(1)) return TNC_ERR_CUDA;
         if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_N, nq, ms, nbb, mone, W2t, nbb, Vt, ms, one, Qs, m, tcws,
                                 L.tcws_bytes, st))
           return rc;
