@@ -395,9 +395,9 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // Q <- (I - V T V^H) Q for the panels in reverse order.  In the transposed
 // working layout (rows of Bt / Qt are columns of A / Q) each update is
 //   Wt = X2t conj(V) ,  W2t = Wt op(T) ,  X2t -= W2t Vt
-// with the long dimension as GEMM rows.  FP32-class types run these GEMMs on
-// the tensor cores (TF32 split products, FP32-class accuracy), FP64 types on
-// the CUDA-core GEMM.
+// with the long dimension as GEMM rows, all on the CUDA-core GEMM (the
+// products have K = 64 or a narrow output; FP32 rounding keeps the
+// reflectors orthogonal to FP32 accuracy).
 template <typename T>
 static int dtype_of() {
   return sizeof(T) == 4 ? TNC_F32 : (sizeof(T) == 8 ? (traits<T>::is_complex ? TNC_C64 : TNC_F64) : TNC_C128);
@@ -409,7 +409,7 @@ constexpr int64_t kQrBlockedMin = 2 * kQrNB;  // k below this: unblocked dataflo
 constexpr int64_t kQrSplitK = 128;  // K chunk of the split-K products
 
 struct QrLayout {
-  size_t bt, tau, flags, sync, qt, vt, s, tm, wt, w2t, part, tcws, tcws_bytes, total;
+  size_t bt, tau, flags, sync, qt, vt, sm, wt, w2t, part, total;
   bool blocked;
 };
 static QrLayout qr_layout(int64_t m, int64_t n, int dt) {
@@ -423,24 +423,15 @@ static QrLayout qr_layout(int64_t m, int64_t n, int dt) {
   L.flags = off; off = align256(off + (size_t)k * sizeof(int));
   L.sync = off; off = align256(off + sizeof(SyncWords));
   L.qt = off; off = align256(off + (size_t)k * m * es);
-  L.vt = L.s = L.tm = L.wt = L.w2t = L.part = L.tcws = off;
-  L.tcws_bytes = 0;
+  L.vt = L.sm = L.wt = L.w2t = L.part = off;
   if (L.blocked) {
     const int64_t nblk = (k + kQrNB - 1) / kQrNB;
     const int64_t rows = n > k ? n : k;
     L.vt = off; off = align256(off + (size_t)kQrNB * m * es);
-    L.s = off; off = align256(off + (size_t)kQrNB * kQrNB * es);
-    L.tm = off; off = align256(off + (size_t)nblk * kQrNB * kQrNB * es);
+    L.sm = off; off = align256(off + (size_t)nblk * kQrNB * kQrNB * es);
     L.wt = off; off = align256(off + (size_t)rows * kQrNB * es);
     L.w2t = off; off = align256(off + (size_t)rows * kQrNB * es);
     L.part = off; off = align256(off + (size_t)((m + kQrSplitK - 1) / kQrSplitK) * rows * kQrNB * es);
-    if (dt == TNC_F32 || dt == TNC_C64) {  // tensor-core GEMMs: split-operand workspace
-      size_t a = 0, b = 0;
-      tnc_gemm_tc_workspace_size(dt, rows, kQrNB, m, 1, &a);
-      tnc_gemm_tc_workspace_size(dt, rows, m, kQrNB, 1, &b);
-      L.tcws_bytes = a > b ? a : b;
-    }
-    L.tcws = off; off = align256(off + L.tcws_bytes);
   }
   L.total = off;
   return L;
@@ -557,26 +548,6 @@ __global__ void qr_eye_rows(T* Qt, int64_t k, int64_t m) {
   }
 }
 
-// C = alpha op(A) op(B) + beta C: tensor cores for FP32-class types when the
-// product is large enough and the workspace holds its split operands
-template <typename T>
-static int qr_gemm(int opA, int opB, int64_t M, int64_t N, int64_t K, T alpha, const T* A, int64_t lda, const T* B,
-                   int64_t ldb, T beta, T* C, int64_t ldc, void* tcws, size_t tcwb, cudaStream_t st) {
-  if constexpr (sizeof(typename traits<T>::real) == 4) {
-    if (tcws != nullptr && M >= 64 && N >= 64 && K >= 32 && (double)M * N * K >= (double)(1 << 21)) {
-      size_t need = 0;
-      if (tnc_gemm_tc_workspace_size(dtype_of<T>(), M, N, K, 1, &need) == TNC_OK && need <= tcwb) {
-        double a[2], b[2];
-        if constexpr (traits<T>::is_complex) { a[0] = alpha.re; a[1] = alpha.im; b[0] = beta.re; b[1] = beta.im; }
-        else { a[0] = alpha; a[1] = 0; b[0] = beta; b[1] = 0; }
-        return tnc_gemm_tc(dtype_of<T>(), opA, opB, M, N, K, a, A, lda, 0, B, ldb, 0, b, C, ldc, 0, 1, tcws, tcwb,
-                           st);
-      }
-    }
-  }
-  return gemm_launch<T>(opA, opB, M, N, K, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, st);
-}
-
 // C (M x N, ld ldc) = op(A) op(B) with A (M x K, row-major, opA N or R) and B
 // (N x K, row-major, opB T or C): the K range is cut into chunks of kQrSplitK,
 // each chunk one member of a batched CUDA-core GEMM into P, then the partial
@@ -689,12 +660,11 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
     if (launch_status(launches)) return TNC_ERR_CUDA;
   } else {
     T* Vt = (T*)(w + L.vt);
-    T* Sall = (T*)(w + L.tm);  // S = V^H V of every panel
+    T* Sall = (T*)(w + L.sm);  // S = V^H V of every panel
     T* Wt = (T*)(w + L.wt);
     T* W2t = (T*)(w + L.w2t);
     T* P = (T*)(w + L.part);
-    void* tcws = L.tcws_bytes ? (void*)(w + L.tcws) : nullptr;
-    const T one = one_<T>(), zero = zero_<T>(), mone = zero_<T>() - one_<T>();
+    const T one = one_<T>(), mone = zero_<T>() - one_<T>();
     const int64_t nblk = (k + kQrNB - 1) / kQrNB;
     if (int rc = ensure_form_t_smem<T>()) return rc;
     const size_t tinv_smem = (size_t)(kQrNB * kQrNB + kQrNB) * sizeof(T);
@@ -719,8 +689,8 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
         // W2 = T^H W
         qr_apply_tinv<T><<<grid1d(n2 * 32, 256, 152 * 8), 256, tinv_smem, st>>>(Sb, tau + c0, nbb, Wt, W2t, n2, 1);
         if (launch_status(1)) return TNC_ERR_CUDA;
-        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_N, n2, ms, nbb, mone, W2t, nbb, Vt, ms, one, X2t, m, tcws,
-                                L.tcws_bytes, st))
+        if (int rc = gemm_launch<T>(TNC_OP_N, TNC_OP_N, n2, ms, nbb, mone, W2t, nbb, 0, Vt, ms, 0, one, X2t, m, 0, 1,
+                                    st))
           return rc;
       }
     }
@@ -743,8 +713,7 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
         // W2 = T W
         qr_apply_tinv<T><<<grid1d(nq * 32, 256, 152 * 8), 256, tinv_smem, st>>>(Sb, tau + c0, nbb, Wt, W2t, nq, 0);
         if (launch_status(1)) return TNC_ERR_CUDA;
-        if (int rc = qr_gemm<T>(TNC_OP_N, TNC_OP_N, nq, ms, nbb, mone, W2t, nbb, Vt, ms, one, Qs, m, tcws,
-                                L.tcws_bytes, st))
+        if (int rc = gemm_launch<T>(TNC_OP_N, TNC_OP_N, nq, ms, nbb, mone, W2t, nbb, 0, Vt, ms, 0, one, Qs, m, 0, 1, st))
           return rc;
       }
     }

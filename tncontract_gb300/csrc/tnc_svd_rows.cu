@@ -36,7 +36,7 @@ __device__ __forceinline__ void circle_pair(int64_t np, int64_t r, int64_t i, in
 
 template <typename T>
 struct Rot {
-  typename traits<T>::real c;
+  typename traits<T>::real c, th;  // th = t |g|: the norms move to a - th, b + th
   T se, sec;
   bool apply;
 };
@@ -50,12 +50,13 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
   const R h = abs_(g);
   // rows at the rounding-noise floor (or whose squared norm underflowed) count as converged
   r.apply = (a > noise2) && (b > noise2) && (a > 0) && (b > 0) && (h > rtol * sqrt(a) * sqrt(b));
-  if (!r.apply) { r.c = 1; r.se = zero_<T>(); r.sec = zero_<T>(); return r; }
+  if (!r.apply) { r.c = 1; r.th = 0; r.se = zero_<T>(); r.sec = zero_<T>(); return r; }
   const R tau = (b - a) / (2 * h);
   R t;
   if (fabs(tau) > (R)1e15) t = (R)0.5 / tau;
   else t = (tau >= 0 ? R(1) : R(-1)) / (fabs(tau) + sqrt(R(1) + tau * tau));
   r.c = R(1) / sqrt(R(1) + t * t);
+  r.th = t * h;
   const R s = r.c * t;
   const T e = div_real_(g, h);
   r.se = s * e;
@@ -63,14 +64,17 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
   return r;
 }
 
-// rows x (registers, MAXE per lane) and y (shared memory), one warp
+// rows x (registers, MAXE per lane) and y (shared memory), one warp.  The
+// squared norms a (of x) and *b (of y) are carried, not recomputed: only
+// g = <x, y> is reduced, and a rotation moves them to a - t|g|, b + t|g|
+// (exact in exact arithmetic; recomputed from the rows once per sweep).
 template <typename T, int MAXE>
 __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, typename traits<T>::real rtol,
-                                                typename traits<T>::real noise2) {
+                                                typename traits<T>::real noise2, typename traits<T>::real& a,
+                                                typename traits<T>::real* b) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
-  R a = 0, b = 0;
-  T g = zero_<T>();
+  T g0 = zero_<T>(), g1 = zero_<T>();
   T yr[MAXE];  // the partner row stays in registers between the two passes
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
@@ -79,14 +83,12 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
   }
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
-    a += abs2_(x[u]);
-    b += abs2_(yr[u]);
-    fma_(g, x[u], conj_(yr[u]));
+    if (u & 1) fma_(g1, x[u], conj_(yr[u]));
+    else fma_(g0, x[u], conj_(yr[u]));
   }
-  a = warp_sum(a);
-  b = warp_sum(b);
-  g = warp_sum(g);
-  const Rot<T> r = make_rot<T>(a, b, g, rtol, noise2);
+  const T g = warp_sum(g0 + g1);
+  const R bb = *b;
+  const Rot<T> r = make_rot<T>(a, bb, g, rtol, noise2);
   if (!r.apply) return false;
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
@@ -95,34 +97,50 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
     x[u] = r.c * xv - r.se * yr[u];
     if (k < L) y[k] = r.sec * xv + r.c * yr[u];
   }
+  a = a - r.th;
+  if (lane == 0) *b = bb + r.th;
   return true;
 }
 
-// rows x and y both in shared memory, one warp
+// rows x and y both in shared memory, one warp; squared norms *a, *b carried
 template <typename T>
 __device__ __forceinline__ bool rotate_smem_smem(T* x, T* y, int64_t L, typename traits<T>::real rtol,
-                                                 typename traits<T>::real noise2) {
+                                                 typename traits<T>::real noise2, typename traits<T>::real* a,
+                                                 typename traits<T>::real* b) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
-  R a = 0, b = 0;
-  T g = zero_<T>();
-  for (int64_t k = lane; k < L; k += 32) {
-    const T xv = x[k], yv = y[k];
-    a += abs2_(xv);
-    b += abs2_(yv);
-    fma_(g, xv, conj_(yv));
+  T g0 = zero_<T>(), g1 = zero_<T>();
+  int64_t k = lane;
+  for (; k + 32 < L; k += 64) {
+    fma_(g0, x[k], conj_(y[k]));
+    fma_(g1, x[k + 32], conj_(y[k + 32]));
   }
-  a = warp_sum(a);
-  b = warp_sum(b);
-  g = warp_sum(g);
-  const Rot<T> r = make_rot<T>(a, b, g, rtol, noise2);
+  if (k < L) fma_(g0, x[k], conj_(y[k]));
+  const T g = warp_sum(g0 + g1);
+  const R aa = *a, bb = *b;
+  const Rot<T> r = make_rot<T>(aa, bb, g, rtol, noise2);
   if (!r.apply) return false;
-  for (int64_t k = lane; k < L; k += 32) {
-    const T xv = x[k], yv = y[k];
-    x[k] = r.c * xv - r.se * yv;
-    y[k] = r.sec * xv + r.c * yv;
+  for (int64_t kk = lane; kk < L; kk += 32) {
+    const T xv = x[kk], yv = y[kk];
+    x[kk] = r.c * xv - r.se * yv;
+    y[kk] = r.sec * xv + r.c * yv;
   }
+  __syncwarp();
+  if (lane == 0) { *a = aa - r.th; *b = bb + r.th; }
+  __syncwarp();
   return true;
+}
+
+// squared norm of one row (length L) by one warp, every lane gets it
+template <typename T>
+__device__ __forceinline__ typename traits<T>::real warp_row_norm2(const T* x, int64_t L) {
+  typedef typename traits<T>::real R;
+  const int lane = threadIdx.x & 31;
+  R a0 = 0, a1 = 0;
+  int64_t k = lane;
+  for (; k + 32 < L; k += 64) { a0 += abs2_(x[k]); a1 += abs2_(x[k + 32]); }
+  if (k < L) a0 += abs2_(x[k]);
+  return warp_sum(a0 + a1);
 }
 
 // cooperative copy of rows [row0, row0 + cnt) of W (row length L) to/from smem
@@ -155,10 +173,11 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
 template <typename T, int MAXE>
 __global__ void __launch_bounds__(256)
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
-                    unsigned* counters, SyncWords* sw, int* info) {
+                    typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sB = reinterpret_cast<T*>(smem_raw);
+  __shared__ R sn[32];  // squared norms of the shared-memory rows
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nb = (nr + h - 1) / h;
   const int64_t nbp = nb + (nb & 1);
@@ -177,16 +196,24 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
       const int cnt = (int)((nr - row0) < h ? (nr - row0) : h);
       rows_to_smem(W, row0, cnt, L, sB);
       __syncthreads();
+      // exact squared norms once per sweep (the rounds carry them)
+      if (warp < cnt) {
+        const R a = warp_row_norm2(sB + (int64_t)warp * L, L);
+        if (lane == 0) sn[warp] = a;
+      }
+      __syncthreads();
       const int hp = h + (h & 1);
       for (int rr = 0; rr < hp - 1; ++rr) {
         if (warp < hp / 2) {
           int64_t p, q;
           circle_pair(hp, rr, warp, p, q);
-          if (p < cnt && q < cnt) rot += rotate_smem_smem(sB + p * L, sB + q * L, L, rtol, noise2) ? 1u : 0u;
+          if (p < cnt && q < cnt)
+            rot += rotate_smem_smem(sB + p * L, sB + q * L, L, rtol, noise2, &sn[p], &sn[q]) ? 1u : 0u;
         }
         __syncthreads();
       }
       rows_from_smem(W, row0, cnt, L, sB);
+      if (threadIdx.x < cnt) Dn[row0 + threadIdx.x] = sn[threadIdx.x];
       __syncthreads();
     }
     if (!grid_barrier(sw, gridDim.x)) return;
@@ -200,18 +227,22 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
         const bool hasA = rowA < nr;
         const int64_t q0 = Q * h;
         const int cntB = (int)((nr - q0) < h ? (nr - q0) : h);
+        R an = 0;
         if (hasA) {
 #pragma unroll
           for (int u = 0; u < MAXE; ++u) {
             const int64_t k = lane + 32 * u;
             x[u] = (k < L) ? ldcg(W + rowA * L + k) : zero_<T>();
           }
+          an = ldcg(Dn + rowA);
         }
         rows_to_smem(W, q0, cntB, L, sB);
+        if (threadIdx.x < cntB) sn[threadIdx.x] = ldcg(Dn + q0 + threadIdx.x);
         __syncthreads();
         for (int s = 0; s < h; ++s) {
           const int j = (warp + s) % h;
-          if (hasA && j < cntB) rot += rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol, noise2) ? 1u : 0u;
+          if (hasA && j < cntB)
+            rot += rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol, noise2, an, &sn[j]) ? 1u : 0u;
           __syncthreads();
         }
         if (hasA) {
@@ -220,8 +251,10 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
             const int64_t k = lane + 32 * u;
             if (k < L) stcg(W + rowA * L + k, x[u]);
           }
+          if (lane == 0) stcg(Dn + rowA, an);
         }
         rows_from_smem(W, q0, cntB, L, sB);
+        if (threadIdx.x < cntB) stcg(Dn + q0 + threadIdx.x, sn[threadIdx.x]);
         __syncthreads();
       }
       if (!grid_barrier(sw, gridDim.x)) return;
@@ -291,12 +324,13 @@ __global__ void gather_rows_kernel(const T* src, int64_t L, const int64_t* order
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-struct RowsLayout { size_t d, frob2, counters, sync, total; };
+struct RowsLayout { size_t d, dn, frob2, counters, sync, total; };
 static const int kRowsMaxSweeps = 100;
 static RowsLayout rows_layout(int64_t nr, size_t rs) {
   RowsLayout Ly;
   size_t off = 0;
   Ly.d = off; off = align256(off + (size_t)nr * rs);
+  Ly.dn = off; off = align256(off + (size_t)nr * rs);
   Ly.frob2 = off; off = align256(off + sizeof(double));
   Ly.counters = off; off = align256(off + kRowsMaxSweeps * sizeof(unsigned));
   Ly.sync = off; off = align256(off + sizeof(SyncWords));
@@ -331,7 +365,7 @@ static int ensure_smem_attr() {
 
 template <typename T, int MAXE>
 static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, const double* frob2,
-                        unsigned* counters, SyncWords* sw, int* info, cudaStream_t st) {
+                        typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info, cudaStream_t st) {
   const size_t smem = (size_t)h * L * sizeof(T);
   const void* fn = (const void*)jacobi_block_kernel<T, MAXE>;
   if (smem > kMaxHalfBlockBytes) return TNC_ERR_ARG;
@@ -350,7 +384,7 @@ static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, 
   int h_ = h, ms_ = ms;
   double tol_ = tol;
   void* args[] = {(void*)&W, (void*)&nr_, (void*)&L_, (void*)&h_, (void*)&ms_, (void*)&tol_,
-                  (void*)&frob2, (void*)&counters, (void*)&sw, (void*)&info};
+                  (void*)&frob2, (void*)&Dn, (void*)&counters, (void*)&sw, (void*)&info};
   if (cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, st) != cudaSuccess) return TNC_ERR_CUDA;
   return TNC_OK;
 }
@@ -373,6 +407,7 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
   unsigned* counters = (unsigned*)(w + Ly.counters);
   SyncWords* sw = (SyncWords*)(w + Ly.sync);
   double* frob2 = (double*)(w + Ly.frob2);
+  R* Dn = (R*)(w + Ly.dn);
   int s;
   if (tall) {
     int64_t shp[2] = {m, n};
@@ -399,10 +434,14 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
     while (h > 2 && h / 2 >= nr) h >>= 1;
     const bool big = sizeof(T) >= 16;
     int rc;
-    if (L <= 256) rc = launch_block<T, 8>(W, nr, L, h, max_sweeps, tol, frob2, counters, sw, info, st);
-    else if (L <= 512) rc = launch_block<T, 16>(W, nr, L, h, max_sweeps, tol, frob2, counters, sw, info, st);
-    else if (L <= 1024 && !big) rc = launch_block<T, 32>(W, nr, L, h, max_sweeps, tol, frob2, counters, sw, info, st);
-    else return TNC_ERR_ARG;  // rows too long for the register-resident half block
+    if (L <= 256) rc = launch_block<T, 8>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+    else if (L <= 512) rc = launch_block<T, 16>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+    else if (L <= 1024 && !big) {
+      if constexpr (sizeof(T) < 16) rc = launch_block<T, 32>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+      else return TNC_ERR_ARG;
+    } else {
+      return TNC_ERR_ARG;  // rows too long for the register-resident half block
+    }
     if (rc) return rc;
     ++launched;
   }
