@@ -155,3 +155,32 @@ def sweep_flops(N, d, D, chi, complex_=True, chi_in=None):
         f[key] *= scale
     f["total"] = sum(f.values())
     return f
+
+
+def instance_flops(N, d, chi, complex_=True):
+    """Estimated flops of one left-canonise + svd_compress of an N-site MPS
+    (phys d, bond chi): the sweep count above with no MPO (D = 1)."""
+    return sweep_flops(N, d, 1, chi, complex_=complex_)["total"]
+
+
+def spec_flops(spec):
+    """instance_flops of one (N, d, chi, dtype, seed) spec of the uneven batch."""
+    N, d, chi, dt, _seed = spec
+    return instance_flops(N, d, chi, bool(np.iscomplexobj(np.zeros(0, dt))))
+
+
+def partition_by_flops(specs, world):
+    """Split independent instances across ``world`` ranks, balancing the
+    estimated flops (greedy longest-processing-time: heaviest first, each to
+    the least-loaded rank).  ``specs`` are (N, d, chi, dtype, seed) tuples;
+    returns one sorted list of instance indices per rank.  Deterministic, so
+    every rank computes the same split without communicating."""
+    cost = [spec_flops(sp) for sp in specs]
+    order = sorted(range(len(specs)), key=lambda i: (-cost[i], i))
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        parts[r].append(i)
+        load[r] += cost[i]
+    return [sorted(p) for p in parts]
