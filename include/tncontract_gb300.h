@@ -226,10 +226,10 @@ int tnc_svd_noalloc(int dtype, int64_t m, int64_t n, const void *A,
  * buffer), S = row norms sorted descending (real type of dtype) and order
  * (int64: order[i] = row of W holding the i-th singular triplet).  For a wide
  * A, rows order[:k] of W are S_k V_k^H and U_k = A (S_k V_k^H)^H S_k^-2; for
- * a tall A they are S_k U_k^H and S_k V_k^H = U_k^H A.  block_rows (2, 4 or
- * 8; anything else selects 8) is the half-block height, chosen per shape
- * by the caller's autotuner.  max(m,n) <= 1024
- * (512 for F64/C128).  info as for tnc_svd. */
+ * a tall A they are S_k U_k^H and S_k V_k^H = U_k^H A.  block_rows (2, 4, 8,
+ * or 16 for rows up to 512 of types up to 8 bytes; anything else selects 8)
+ * is the half-block height, chosen per shape by the caller's autotuner.
+ * max(m,n) <= 1024 (512 for F64/C128).  info as for tnc_svd. */
 int tnc_svd_rows_workspace_size(int dtype, int64_t m, int64_t n, size_t *bytes);
 int tnc_svd_rows(int dtype, int64_t m, int64_t n, const void *A, void *W,
                  void *S, int64_t *order, int max_sweeps, double tol,

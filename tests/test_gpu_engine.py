@@ -20,7 +20,8 @@ def rnd(rng, shape, dt):
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64, np.complex64, np.complex128])
 @pytest.mark.parametrize("shape", [(2, 2), (3, 40), (40, 3), (33, 65), (96, 200), (260, 120), (512, 768)])
-def test_svd_rows(gpu, dt, shape):
+@pytest.mark.parametrize("block_rows", [None, 16])
+def test_svd_rows(gpu, dt, shape, block_rows):
     from tncontract_gb300 import _ops
     if np.dtype(dt).itemsize * (2 if np.iscomplexobj(np.zeros(0, dt)) else 1) >= 16 and max(shape) > 512:
         pytest.skip("FP64 complex rows above 512 use the accumulating SVD")
@@ -28,7 +29,7 @@ def test_svd_rows(gpu, dt, shape):
         pytest.skip("FP64 rows above 512 use the accumulating SVD")
     rng = np.random.default_rng(11)
     A = rnd(rng, shape, dt)
-    W, S, order, info = _ops.svd_rows(torch.from_numpy(A).cuda())
+    W, S, order, info = _ops.svd_rows(torch.from_numpy(A).cuda(), block_rows=block_rows)
     assert int(info[0].item()) == 0
     s = S.cpu().numpy()
     s_ref = np.linalg.svd(A.astype(np.complex128), compute_uv=False)

@@ -163,8 +163,8 @@ __device__ __forceinline__ T shfl_T(T v, int src) {
 
 // value at row i of a register-resident column, broadcast to the warp
 template <typename T, int E>
-__device__ __forceinline__ T reg_get(const T (&x)[E], int64_t i) {
-  const int64_t slot = i >> 5;
+__device__ __forceinline__ T reg_get(const T (&x)[E], int i) {
+  const int slot = i >> 5;
   T a = zero_<T>();
 #pragma unroll
   for (int u = 0; u < E; ++u)
@@ -175,13 +175,13 @@ __device__ __forceinline__ T reg_get(const T (&x)[E], int64_t i) {
 // larfg on the register column: entries > c scaled to v, entry c = beta.
 // Norm with four independent partial sums (short dependency chains).
 template <typename T, int E>
-__device__ __forceinline__ T make_reflector_reg(T (&x)[E], int64_t c, int64_t m) {
+__device__ __forceinline__ T make_reflector_reg(T (&x)[E], int c, int m) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
   R xn0 = 0, xn1 = 0, xn2 = 0, xn3 = 0;
 #pragma unroll
   for (int u = 0; u < E; ++u) {
-    const int64_t i = lane + 32 * u;
+    const int i = lane + 32 * u;
     const R a = (i > c && i < m) ? abs2_(x[u]) : R(0);
     if ((u & 3) == 0) xn0 += a; else if ((u & 3) == 1) xn1 += a; else if ((u & 3) == 2) xn2 += a; else xn3 += a;
   }
@@ -195,7 +195,7 @@ __device__ __forceinline__ T make_reflector_reg(T (&x)[E], int64_t c, int64_t m)
     const T scal = div_(one_<T>(), alpha - betaT);
 #pragma unroll
     for (int u = 0; u < E; ++u) {
-      const int64_t i = lane + 32 * u;
+      const int i = lane + 32 * u;
       if (i > c && i < m) x[u] = scal * x[u];
       else if (i == c) x[u] = betaT;
     }
@@ -209,7 +209,7 @@ __device__ __forceinline__ T make_reflector_reg(T (&x)[E], int64_t c, int64_t m)
 // the L2 latency overlapped without a full register copy of v); the dot
 // product runs four independent partial sums.
 template <typename T, int E, bool GLOBAL>
-__device__ __forceinline__ void apply_stream(T (&x)[E], const T* v, T tau, int64_t c, int64_t m) {
+__device__ __forceinline__ void apply_stream(T (&x)[E], const T* v, T tau, int c, int m) {
   constexpr int C = (E % 16 == 0 && E < 48) ? 16 : 8;
   const int lane = threadIdx.x & 31;
   T w0 = zero_<T>(), w1 = zero_<T>(), w2 = zero_<T>(), w3 = zero_<T>();
@@ -218,13 +218,13 @@ __device__ __forceinline__ void apply_stream(T (&x)[E], const T* v, T tau, int64
     T vc[C];
 #pragma unroll
     for (int q = 0; q < C; ++q) {
-      const int64_t i = lane + 32 * (u0 + q);
+      const int i = lane + 32 * (u0 + q);
       vc[q] = (i > c && i < m) ? (GLOBAL ? ldcg(v + i) : v[i]) : zero_<T>();
     }
 #pragma unroll
     for (int q = 0; q < C; ++q) {
       const int u = u0 + q;
-      const int64_t i = lane + 32 * u;
+      const int i = lane + 32 * u;
       if (i == c) w0 += x[u];
       else if ((q & 3) == 0) fma_(w0, conj_(vc[q]), x[u]);
       else if ((q & 3) == 1) fma_(w1, conj_(vc[q]), x[u]);
@@ -239,13 +239,13 @@ __device__ __forceinline__ void apply_stream(T (&x)[E], const T* v, T tau, int64
     T vc[C];
 #pragma unroll
     for (int q = 0; q < C; ++q) {
-      const int64_t i = lane + 32 * (u0 + q);
+      const int i = lane + 32 * (u0 + q);
       vc[q] = (i > c && i < m) ? (GLOBAL ? ldcg(v + i) : v[i]) : zero_<T>();
     }
 #pragma unroll
     for (int q = 0; q < C; ++q) {
       const int u = u0 + q;
-      const int64_t i = lane + 32 * u;
+      const int i = lane + 32 * u;
       if (i == c) x[u] = x[u] - f;
       else x[u] = x[u] - f * vc[q];  // vc is 0 outside (c, m)
     }
@@ -255,12 +255,12 @@ __device__ __forceinline__ void apply_stream(T (&x)[E], const T* v, T tau, int64
 // x <- H_c^H x with v held in registers vv (v_c = 1 implied); used by the
 // Q formation kernel below
 template <typename T, int E>
-__device__ __forceinline__ void apply_reg(T (&x)[E], const T (&vv)[E], T tau, int64_t c, int64_t m) {
+__device__ __forceinline__ void apply_reg(T (&x)[E], const T (&vv)[E], T tau, int c, int m) {
   const int lane = threadIdx.x & 31;
   T w0 = zero_<T>(), w1 = zero_<T>();
 #pragma unroll
   for (int u = 0; u < E; ++u) {
-    const int64_t i = lane + 32 * u;
+    const int i = lane + 32 * u;
     if (i == c) w0 += x[u];
     else if (i > c && i < m) {
       if (u & 1) fma_(w1, conj_(vv[u]), x[u]);
@@ -271,7 +271,7 @@ __device__ __forceinline__ void apply_reg(T (&x)[E], const T (&vv)[E], T tau, in
   const T f = conj_(tau) * w;
 #pragma unroll
   for (int u = 0; u < E; ++u) {
-    const int64_t i = lane + 32 * u;
+    const int i = lane + 32 * u;
     if (i == c) x[u] = x[u] - f;
     else if (i > c && i < m) x[u] = x[u] - f * vv[u];
   }
@@ -283,6 +283,7 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
   __shared__ T sv[2 * 32 * E];
   __shared__ T stau[2];
   const int64_t k = m < n ? m : n;
+  const int mi = (int)m;  // rows <= 32 * E
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t p0 = (int64_t)blockIdx.x * kPanel;  // first column of the panel
   const int64_t j = p0 + warp;                      // my column
@@ -291,8 +292,8 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
   if (has) {
 #pragma unroll
     for (int u = 0; u < E; ++u) {
-      const int64_t i = lane + 32 * u;
-      x[u] = (i < m) ? Bt[j * ld + i] : zero_<T>();
+      const int i = lane + 32 * u;
+      x[u] = (i < mi) ? Bt[j * ld + i] : zero_<T>();
     }
   }
   // reflectors of earlier panels, as they are published (read from L2)
@@ -300,7 +301,7 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
   if (has) {
     for (int64_t c = 0; c < cend; ++c) {
       if (!warp_wait_flag(&flags[c], sw)) break;
-      apply_stream<T, E, true>(x, Bt + c * ld, ldcg(tau + c), c, m);
+      apply_stream<T, E, true>(x, Bt + c * ld, ldcg(tau + c), (int)c, mi);
     }
   }
   __syncthreads();
@@ -312,11 +313,11 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
   // (look-ahead), so each column costs one barrier.
   const int64_t nw = (k - p0) < kPanel ? (k - p0) : kPanel;
   if (nw > 0 && warp == 0) {
-    const T t = make_reflector_reg(x, p0, m);
+    const T t = make_reflector_reg(x, (int)p0, mi);
 #pragma unroll
     for (int u = 0; u < E; ++u) {
-      const int64_t i = lane + 32 * u;
-      if (i < m) sv[i] = x[u];
+      const int i = lane + 32 * u;
+      if (i < mi) sv[i] = x[u];
     }
     if (lane == 0) stau[0] = t;
   }
@@ -327,22 +328,22 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
     if (warp == w) {
 #pragma unroll
       for (int u = 0; u < E; ++u) {
-        const int64_t i = lane + 32 * u;
-        if (i >= c && i < m) stcg(Bt + c * ld + i, x[u]);
+        const int i = lane + 32 * u;
+        if (i >= (int)c && i < mi) stcg(Bt + c * ld + i, x[u]);
       }
       if (lane == 0) stcg(tau + c, stau[b]);
       __threadfence();
       __syncwarp();
       if (lane == 0) atomicExch(&flags[c], 1);
     } else if (has && warp > w) {
-      apply_stream<T, E, false>(x, sv + b * (32 * E), stau[b], c, m);
+      apply_stream<T, E, false>(x, sv + b * (32 * E), stau[b], (int)c, mi);
       if (warp == w + 1 && w + 1 < nw) {
-        const T t = make_reflector_reg(x, c + 1, m);
+        const T t = make_reflector_reg(x, (int)c + 1, mi);
         T* nb = sv + (b ^ 1) * (32 * E);
 #pragma unroll
         for (int u = 0; u < E; ++u) {
-          const int64_t i = lane + 32 * u;
-          if (i < m) nb[i] = x[u];
+          const int i = lane + 32 * u;
+          if (i < mi) nb[i] = x[u];
         }
         if (lane == 0) stau[b ^ 1] = t;
       }
@@ -351,8 +352,8 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
   if (has) {
 #pragma unroll
     for (int u = 0; u < E; ++u) {
-      const int64_t i = lane + 32 * u;
-      if (i < m) Bt[j * ld + i] = x[u];
+      const int i = lane + 32 * u;
+      if (i < mi) Bt[j * ld + i] = x[u];
     }
   }
 }
@@ -374,7 +375,7 @@ qr_form_q_reg_kernel(const T* __restrict__ Bt, int64_t m, int64_t k, const T* __
         vv[u] = (i > c && i < m) ? Bt[c * m + i] : zero_<T>();
       }
       // H_c (not conjugated): x -= tau (v^H x) v
-      apply_reg(x, vv, conj_(tau[c]), c, m);
+      apply_reg(x, vv, conj_(tau[c]), (int)c, (int)m);
     }
 #pragma unroll
     for (int u = 0; u < E; ++u) {
@@ -507,7 +508,7 @@ __global__ void qr_apply_tinv(const T* __restrict__ S, const T* __restrict__ tau
 // Dynamic shared memory of qr_apply_tinv beyond the 48 KB default
 // (complex128): raised once per device.
 template <typename T>
-static int ensure_form_t_smem() {
+static int ensure_tinv_smem() {
   constexpr size_t bytes = (size_t)(kQrNB * kQrNB + kQrNB) * sizeof(T);
   if constexpr (bytes <= 48 * 1024) {
     return TNC_OK;
@@ -666,7 +667,7 @@ static int qr_factor_bt(int64_t m, int64_t n, T* Q, bool want_qt, T* R, const Qr
     T* P = (T*)(w + L.part);
     const T one = one_<T>(), mone = zero_<T>() - one_<T>();
     const int64_t nblk = (k + kQrNB - 1) / kQrNB;
-    if (int rc = ensure_form_t_smem<T>()) return rc;
+    if (int rc = ensure_tinv_smem<T>()) return rc;
     const size_t tinv_smem = (size_t)(kQrNB * kQrNB + kQrNB) * sizeof(T);
     for (int64_t b = 0; b < nblk; ++b) {
       const int64_t c0 = b * kQrNB;

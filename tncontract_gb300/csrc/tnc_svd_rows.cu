@@ -58,7 +58,8 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
   r.c = R(1) / sqrt(R(1) + t * t);
   r.th = t * h;
   const R s = r.c * t;
-  const T e = div_real_(g, h);
+  const R inv_h = R(1) / h;  // one division for both parts of e = g / |g|
+  const T e = isfinite(inv_h) ? g * inv_h : div_real_(g, h);
   r.se = s * e;
   r.sec = s * conj_(e);
   return r;
@@ -74,12 +75,13 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
                                                 typename traits<T>::real* b) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
+  const int Li = (int)L;  // row length <= 32 * MAXE
   T g0 = zero_<T>(), g1 = zero_<T>();
   T yr[MAXE];  // the partner row stays in registers between the two passes
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
-    const int64_t k = lane + 32 * u;
-    yr[u] = (k < L) ? y[k] : zero_<T>();
+    const int k = lane + 32 * u;
+    yr[u] = (k < Li) ? y[k] : zero_<T>();
   }
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
@@ -92,10 +94,10 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
   if (!r.apply) return false;
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
-    const int64_t k = lane + 32 * u;
+    const int k = lane + 32 * u;
     const T xv = x[u];
     x[u] = r.c * xv - r.se * yr[u];
-    if (k < L) y[k] = r.sec * xv + r.c * yr[u];
+    if (k < Li) y[k] = r.sec * xv + r.c * yr[u];
   }
   a = a - r.th;
   if (lane == 0) *b = bb + r.th;
@@ -170,8 +172,8 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
   for (int64_t e = threadIdx.x; e < total; e += blockDim.x) stcg(W + row0 * L + e, s[e]);
 }
 
-template <typename T, int MAXE>
-__global__ void __launch_bounds__(256)
+template <typename T, int MAXE, int MAXT>
+__global__ void __launch_bounds__(MAXT)
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
                     typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
@@ -349,27 +351,27 @@ template <> int dtype_code<c128>() { return TNC_C128; }
 // different row lengths share the setting).
 static const size_t kMaxHalfBlockBytes = 200 * 1024;
 
-template <typename T, int MAXE>
+template <typename T, int MAXE, int MAXT>
 static int ensure_smem_attr() {
   static std::atomic<unsigned long long> done_mask{0};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TNC_ERR_CUDA;
   const unsigned long long bit = 1ull << (dev & 63);
   if (done_mask.load() & bit) return TNC_OK;
-  if (cudaFuncSetAttribute((const void*)jacobi_block_kernel<T, MAXE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute((const void*)jacobi_block_kernel<T, MAXE, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)kMaxHalfBlockBytes) != cudaSuccess)
     return TNC_ERR_CUDA;
   done_mask.fetch_or(bit);
   return TNC_OK;
 }
 
-template <typename T, int MAXE>
+template <typename T, int MAXE, int MAXT>
 static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, const double* frob2,
                         typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info, cudaStream_t st) {
   const size_t smem = (size_t)h * L * sizeof(T);
-  const void* fn = (const void*)jacobi_block_kernel<T, MAXE>;
-  if (smem > kMaxHalfBlockBytes) return TNC_ERR_ARG;
-  if (int rc = ensure_smem_attr<T, MAXE>()) return rc;
+  const void* fn = (const void*)jacobi_block_kernel<T, MAXE, MAXT>;
+  if (smem > kMaxHalfBlockBytes || 32 * h > MAXT) return TNC_ERR_ARG;
+  if (int rc = ensure_smem_attr<T, MAXE, MAXT>()) return rc;
   const int threads = 32 * h;
   int cap = coop_capacity(fn, threads, smem);
   if (cap <= 0) return TNC_ERR_CUDA;
@@ -428,16 +430,27 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
     ++launched;
     // half-block height: 16 rows (fewest barriers) when the shared-memory half
     // block and the register row fit, else smaller
+    // (16: 512-thread CTAs, rows up to 512 and element types up to 8 bytes)
     int h = 8;
     if (block_rows == 2 || block_rows == 4 || block_rows == 8) h = block_rows;
+    if (block_rows == 16 && L <= 512 && sizeof(T) <= 8) h = 16;
     while (h > 2 && (size_t)h * L * sizeof(T) > kMaxHalfBlockBytes) h >>= 1;
     while (h > 2 && h / 2 >= nr) h >>= 1;
     const bool big = sizeof(T) >= 16;
     int rc;
-    if (L <= 256) rc = launch_block<T, 8>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
-    else if (L <= 512) rc = launch_block<T, 16>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
-    else if (L <= 1024 && !big) {
-      if constexpr (sizeof(T) < 16) rc = launch_block<T, 32>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+    if (h == 16) {
+      if constexpr (sizeof(T) <= 8) {
+        if (L <= 256) rc = launch_block<T, 8, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+        else rc = launch_block<T, 16, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+      } else {
+        return TNC_ERR_ARG;
+      }
+    } else if (L <= 256) {
+      rc = launch_block<T, 8, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+    } else if (L <= 512) {
+      rc = launch_block<T, 16, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+    } else if (L <= 1024 && !big) {
+      if constexpr (sizeof(T) < 16) rc = launch_block<T, 32, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
       else return TNC_ERR_ARG;
     } else {
       return TNC_ERR_ARG;  // rows too long for the register-resident half block
