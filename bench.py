@@ -36,6 +36,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_SITES, PHYS, MPO_D, CHI = 64, 2, 3, 256
+# admission stagger of the work queue (seconds between workers' first jobs):
+# identical instances started together run their QR and SVD phases in
+# lockstep and contend for the same resources at the same time
+STAGGER = 0.025
 METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, complex128)"
 # dram bytes (read + write) per call of the dominant native op at the
 # workload's bulk shape (the Jacobi kernel of tnc_svd_rows on the 512 x 512
@@ -271,48 +275,48 @@ def run_ours(args):
     log_norms = [ln for _, ln in balanced]
     pinned_batch = [[torch.from_numpy(a.astype(np_dt)).pin_memory() for a in sites] for sites, _ in balanced]
     pinned_mpo = [torch.from_numpy(w.astype(np_dt)).pin_memory() for w in host_mpo]
+    # e2e bytes per step: every sweep job copies its instance's sites and the MPO
     h2d = sum(a.numel() * a.element_size() for sites in pinned_batch for a in sites) + \
-        sum(w.numel() * w.element_size() for w in pinned_mpo)
+        B * sum(w.numel() * w.element_size() for w in pinned_mpo)
 
     dev_batch = [E.to_sites(sites, dt) for sites in pinned_batch]
     dev_mpo = E.to_sites(pinned_mpo, dt)
     streams = [torch.cuda.Stream() for _ in range(B)]
 
-    def step():
-        return E.apply_compress_batch(dev_batch, dev_mpo, chi, streams=streams, log_norms=log_norms)
+    # the timed work: K steps of B sweeps as one queue of K*B jobs on B
+    # streams (continuous batching: an instance that finishes its sweep takes
+    # the next one), each sweep one native call (tnc_sweep_apply_compress)
+    import ctypes
+    last = [None] * B
+    OPS = ("tnc_qr", "tnc_qr_r", "tnc_svd_rows")
+
+    def sweep_job(b, prof=None):
+        def job():
+            last[b] = E.apply_compress_native(dev_batch[b], dev_mpo, chi, log_norm_in=log_norms[b], profile=prof)
+        return job
+
+    def run_steps(k, profs=None):
+        jobs = [sweep_job(b, profs[j * B + b] if profs else None) for j in range(k) for b in range(B)]
+        E.run_queue(jobs, B, streams=streams, stagger=STAGGER)
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
 
-    for _ in range(warm - 1):
-        out = step()
+    run_steps(warm)
     barrier()
-    # the last warm-up step is profiled call by call (every C-ABI call between
-    # CUDA events): the breakdown and the dominant op
-    _ops.PROFILE = {}
-    out = step()
-    barrier()
-    summary = _ops.profile_summary(_ops.PROFILE)
-    dom_name = max(summary.items(), key=lambda kv: kv[1][1])[0]
-    # timed region: only the dominant op is bracketed by events
     launches0 = _lib.kernel_launches()
-    _ops.PROFILE = {}
-    _ops.PROFILE_ONLY = {dom_name}
     st = torch.cuda.current_stream()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier()
         ev0.record(st)
-        for _ in range(args.steps):
-            out = step()
+        run_steps(args.steps)
         ev1.record(st)
         barrier()
-    prof = _ops.PROFILE
-    _ops.PROFILE = None
-    _ops.PROFILE_ONLY = None
+    out = last
     launches = _lib.kernel_launches() - launches0
     elapsed = ev0.elapsed_time(ev1) / 1e3
     if world > 1:
@@ -320,27 +324,41 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
     value = world * B * args.steps / elapsed
-    timed = _ops.profile_summary(prof)
+    # per-op durations: one more step of the same workload in which every
+    # sweep brackets its QR, R-only QR and Jacobi calls by CUDA events on its
+    # instance's stream (timing events recorded on 8 concurrent streams slow
+    # the batch down, so the timed region above runs without them)
+    profs = [(ctypes.c_double * 9)() for _ in range(B)]
+    run_steps(1, profs)
+    barrier()
+    timed = {op: (sum(p[3 * o + 1] for p in profs), sum(p[3 * o] for p in profs), sum(p[3 * o + 2] for p in profs))
+             for o, op in enumerate(OPS)}
+    dom_name = max(timed.items(), key=lambda kv: kv[1][1])[0]
 
-    # end to end through the public API: pinned host arrays in, host arrays out
-    def e2e_step():
-        sites = [E.to_sites(s, dt) for s in pinned_batch]
-        mpo = E.to_sites(pinned_mpo, dt)
-        res = E.apply_compress_batch(sites, mpo, chi, streams=streams, log_norms=log_norms)
-        return [[t.cpu().numpy() for t in r] for r in res]
+    # end to end through the public API: pinned host arrays in, host arrays
+    # out, every sweep job copying its own inputs and results
+    e2e_last = [None] * B
 
-    e2e_step()
+    def e2e_job(b):
+        def job():
+            sites = E.to_sites(pinned_batch[b], dt)
+            mpo = E.to_sites(pinned_mpo, dt)
+            r = E.apply_compress_native(sites, mpo, chi, log_norm_in=log_norms[b])
+            e2e_last[b] = [t.cpu().numpy() for t in r]
+        return job
+
+    E.run_queue([e2e_job(b) for b in range(B)], B, streams=streams, stagger=STAGGER)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        res = e2e_step()
+    E.run_queue([e2e_job(b) for _ in range(args.steps) for b in range(B)], B, streams=streams, stagger=STAGGER)
     barrier()
     e2e_el = time.perf_counter() - t0
+    res = e2e_last
     if world > 1:
         t = torch.tensor([e2e_el], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_el = float(t.item())
-    d2h = sum(a.nbytes for r in res for a in r)
+    d2h = sum(a.nbytes for r in res for a in r)  # per step: B instances' results
     e2e_value = world * B * args.steps / e2e_el
 
     # plain FP64 drop-in path (this project's straightforward FP64 method) on
@@ -374,6 +392,7 @@ def run_ours(args):
 
     name = dom_name
     ncalls, ms, flops = timed[name]
+    ncalls = int(ncalls)
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         peak, peak_src = float(peaks["bf16_tflops"]), "measured"
@@ -384,14 +403,15 @@ def run_ours(args):
                "measured bf16 tensor peak, frac_of_fp32_nominal against GB300's nominal FP32 rate "
                "(152 SMs x 128 FMA x 2 x 2.07 GHz = 80.5 TFLOP/s)")
     roofline = {"bound": "tensor", "kernel": name, "launches": ncalls, "achieved": achieved,
-                "measured": "CUDA events around every %s call in the timed region, on its stream (%d streams "
+                "measured": "CUDA events around every %s call, recorded by the native sweep on its instance's "
+                            "stream in one profiled step of the same workload after the timed region (%d streams "
                             "run concurrently, so durations include time shared with other instances)" % (name, B),
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_src,
                 "traffic": TRAFFIC_PER_CALL.get(name), "fp32_nominal_tflops": 80.5,
                 "frac_of_fp32_nominal": achieved / 80.5, "note": fp_note}
-    tot_ms = sum(x[1] for x in summary.values())
-    # from the profiled warm-up step; event intervals on concurrent streams overlap
-    share = {k: round(v[1] / tot_ms, 4) for k, v in summary.items() if v[1] / tot_ms > 1e-4}
+    tot_ms = sum(x[1] for x in timed.values())
+    # of the three factorisation stages' event time in the timed region
+    share = {k: round(v[1] / tot_ms, 4) for k, v in timed.items() if tot_ms > 0}
 
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": warm, "ms_per_step": elapsed / args.steps * 1e3,
@@ -401,12 +421,15 @@ def run_ours(args):
             "config": {"workload": "tfim_apply_svd_compress", "path": "engine (%s)" % args.precision,
                        "batch_per_gpu": B, "nsites": N, "phys_dim": PHYS, "mpo_bond": MPO_D, "chi": chi,
                        "input_dtype": "complex128", "parallelism": "replicas" if world > 1 else "single",
+                       "scheduling": "K steps x %d sweeps as one work queue on %d CUDA streams (continuous "
+                                     "batching), workers admitted %d ms apart, each sweep one native call"
+                                     % (B, B, int(STAGGER * 1e3)),
                        "l2": "inputs larger than L2 (%d MPS of 134 MB in, 1.2 GB applied each)" % B},
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d // 1,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": roofline,
-            "native_call_share": share,
+            "stage_share": share,
             "clocks": clk.summary(),
             "sweep_tflop": W.sweep_flops(N, PHYS, MPO_D, chi)["total"] / 1e12}
     line.update(extra)

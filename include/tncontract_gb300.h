@@ -245,6 +245,38 @@ int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
                     const int64_t *k, int64_t kmax, const void *S, int mode,
                     void *dst, void *stream);
 
+/* ------------------------------------------------------------ the sweep */
+
+/* One MPO.MPS apply + svd_compress sweep run natively on one stream:
+ * contract_mps_mpo followed by MatrixProductState.svd_compress with the
+ * norm restored (onedim_core.py:1691-1708, 463-484; the QR branch of
+ * left_canonise :267-294, the truncating SVD branch :317-343), the retained
+ * rank per bond by the reference's rule (s/s_max > threshold, at most chi,
+ * :332-339) capped at the storage type's rounding-noise floor.  Sites are
+ * (phys, left, right) device arrays; MPO sites (physout, physin, left,
+ * right).  HOST arrays: sites[n_sites] and mpo[n_sites] (device pointers),
+ * mps_bonds[n_sites+1], mpo_bonds[n_sites+1] (both ends 1); out_bonds
+ * [n_sites+1] and out_offsets[n_sites] (byte offset in `work` of each
+ * compressed site, (phys, out_bonds[i], out_bonds[i+1])) are written.
+ * *log_norm: in, the natural log of the input state's norm factor; out, that
+ * of the output.  *folded = 1 when that factor (except its s_max part) was
+ * representable and folded into the first site.  block_rows as for
+ * tnc_svd_rows (0 = 8).  profile (HOST, may be NULL): 9 doubles, for op o
+ * (0 the QR of the left sweep, 1 the R-only QR of M^H, 2 the Jacobi)
+ * profile[3o] += milliseconds (CUDA events on `stream`), [3o+1] += calls,
+ * [3o+2] += the op's fixed algorithmic flops.  Returns TNC_ERR_ARG for a
+ * zero state. */
+int tnc_sweep_workspace_size(int dtype, int n_sites, int64_t d,
+                             const int64_t *mps_bonds, const int64_t *mpo_bonds,
+                             size_t *bytes);
+int tnc_sweep_apply_compress(int dtype, int n_sites, int64_t d,
+                             const void *const *sites, const int64_t *mps_bonds,
+                             const void *const *mpo, const int64_t *mpo_bonds,
+                             int64_t chi, double threshold, int block_rows,
+                             void *work, size_t work_bytes, int64_t *out_bonds,
+                             int64_t *out_offsets, double *log_norm,
+                             int *folded, double *profile, void *stream);
+
 /* ------------------------------------------------------------ learned rank
  * Kernels of the rank predictor (a small MLP trained on singular spectra the
  * plain method produces) and of the randomized-SVD sketch it sizes.  No

@@ -147,6 +147,73 @@ def test_engine_batched(gpu):
         assert 1 - O.fidelity(ref, got) < 1e-6
 
 
+@pytest.mark.parametrize("precision,fid_tol", [("fp64", 1e-10), ("fp32", 1e-6)])
+@pytest.mark.parametrize("case", ["config2_small", "config2_chi128"])
+def test_native_sweep(gpu, precision, fid_tol, case):
+    """tnc_sweep_apply_compress (the whole sweep as one native call) against
+    the oracle and the reference's bond dimensions."""
+    from tncontract_gb300 import engine as E
+    g, m = K.load(case)
+    N, chi = (12, 16) if case == "config2_small" else (64, 128)
+    key = "c2s_m_bonds" if case == "config2_small" else "c2_m_bonds"
+    sites = O.random_mps(0, N, 2, chi, np.complex128, normalise=True)
+    mpo = O.tfim_mpo(N)
+    dt = E.compute_dtype(precision, True)
+    bal, ln = E.balance(sites)
+    st = E.SweepStats()
+    out = E.apply_compress_native(E.to_sites(bal, dt), E.to_sites(mpo, dt), chi, log_norm_in=ln, stats=st)
+    got = [o.cpu().numpy().astype(np.complex128) for o in out]
+    assert [1] + [a.shape[2] for a in got] == m[key]
+    ref = O.apply_compress_sweep(sites, mpo, chi)
+    assert 1 - O.fidelity(ref, got) < fid_tol
+    nr = O.mps_norm(ref)
+    assert abs(O.mps_norm(got) * (1.0 if st.norm_folded else np.exp(st.log_norm - np.log(O.mps_norm(got)))) - nr) \
+        < 10 * fid_tol ** 0.5 * nr
+
+
+def test_native_sweep_real_and_batched(gpu):
+    """Real float64 input through the native sweep, and native sweeps of
+    several instances on the work queue."""
+    from tncontract_gb300 import engine as E
+    sites = O.random_mps(0, 32, 2, 32, np.float64)
+    lc = O.left_canonical_form_mps(sites)
+    ident = [np.eye(2).reshape(2, 2, 1, 1) for _ in range(32)]
+    out = E.apply_compress_native(E.to_sites(lc, torch.float64), E.to_sites(ident, torch.float64), 16)
+    got = [o.cpu().numpy() for o in out]
+    assert 1 - O.fidelity(O.svd_compress_method(lc, 16), got) < 1e-10
+    N, chi = 16, 24
+    mpo = O.tfim_mpo(N)
+    batch_np = [O.random_mps(s, N, 2, chi, np.complex128, normalise=True) for s in range(5)]
+    dt = E.compute_dtype("fp32", True)
+    bal = [E.balance(b) for b in batch_np]
+    Mo = E.to_sites(mpo, dt)
+    outs = E.run_queue([(lambda b=b: E.apply_compress_native(E.to_sites(bal[b][0], dt), Mo, chi,
+                                                             log_norm_in=bal[b][1])) for b in range(5)], 2)
+    torch.cuda.synchronize()
+    for b, out in zip(batch_np, outs):
+        got = [o.cpu().numpy().astype(np.complex128) for o in out]
+        assert 1 - O.fidelity(O.apply_compress_sweep(b, mpo, chi), got) < 1e-6
+
+
+def test_engine_run_queue(gpu):
+    """Continuous batching: 6 sweep jobs on 3 worker streams give the same
+    results as the oracle, in job order."""
+    from tncontract_gb300 import engine as E
+    N, chi = 12, 16
+    mpo = O.tfim_mpo(N)
+    batch_np = [O.random_mps(s, N, 2, chi, np.complex128, normalise=True) for s in range(6)]
+    dt = E.compute_dtype("fp32", True)
+    bal = [E.balance(b) for b in batch_np]
+    Mo = E.to_sites(mpo, dt)
+    jobs = [(lambda b=b: E.apply_compress(E.to_sites(bal[b][0], dt), Mo, chi, log_norm_in=bal[b][1]))
+            for b in range(6)]
+    outs = E.run_queue(jobs, 3)
+    torch.cuda.synchronize()
+    for b, out in zip(batch_np, outs):
+        got = [o.cpu().numpy().astype(np.complex128) for o in out]
+        assert 1 - O.fidelity(O.apply_compress_sweep(b, mpo, chi), got) < 1e-6
+
+
 def test_engine_inner_product(gpu):
     from tncontract_gb300 import engine as E
     a = O.random_mps(5, 10, 3, 7, np.complex128)

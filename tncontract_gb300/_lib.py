@@ -48,6 +48,9 @@ SIGNATURES = {
     "tnc_qr_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_qr": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, C.c_size_t, _vp, _vp],
     "tnc_qr_r_workspace_size": [_int, _i64, _i64, _int, _psz],
+    "tnc_sweep_workspace_size": [_int, _int, _i64, _pi64, _pi64, _psz],
+    "tnc_sweep_apply_compress": [_int, _int, _i64, C.POINTER(_vp), _pi64, C.POINTER(_vp), _pi64, _i64, C.c_double,
+                                 _int, _vp, C.c_size_t, _pi64, _pi64, _pdbl, _pint, _pdbl, _vp],
     "tnc_qr_r": [_int, _i64, _i64, _vp, _int, _vp, _vp, C.c_size_t, _vp, _vp],
     "tnc_svd_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_svd": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, C.c_size_t, _vp, _vp],

@@ -35,6 +35,12 @@ __device__ __forceinline__ cplx<R> div_c(cplx<R> a, cplx<R> b) {
 template <> __device__ __forceinline__ c64 div_(c64 a, c64 b) { return div_c(a, b); }
 template <> __device__ __forceinline__ c128 div_(c128 a, c128 b) { return div_c(a, b); }
 
+// CTA-local barrier over the first `count` threads' warps (count a multiple of
+// 32), id 1..15 (0 is __syncthreads)
+__device__ __forceinline__ void named_barrier(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
 template <typename T> __device__ __forceinline__ typename traits<T>::real imag_(T v) {
   if constexpr (traits<T>::is_complex) return v.im; else return 0;
 }
@@ -252,6 +258,78 @@ __device__ __forceinline__ void apply_stream(T (&x)[E], const T* v, T tau, int c
   }
 }
 
+// The look-ahead step of the owner of column c+1: x <- H_c^H x (v from shared
+// memory) and then the reflector of x at row c+1, in three passes over the
+// register column instead of six: (1) the dot product; (2) the update, the
+// norm of rows > c+1 and row c+1 itself (one shuffle, no select chain);
+// (3) the scaling, written straight to `out` (the next shared buffer).
+template <typename T, int E>
+__device__ __forceinline__ T apply_and_reflect(T (&x)[E], const T* v, T tau, int c, int m, T* out) {
+  typedef typename traits<T>::real R;
+  constexpr int C = (E % 16 == 0 && E < 48) ? 16 : 8;
+  const int lane = threadIdx.x & 31;
+  T w0 = zero_<T>(), w1 = zero_<T>(), w2 = zero_<T>(), w3 = zero_<T>();
+#pragma unroll
+  for (int u0 = 0; u0 < E; u0 += C) {
+    T vc[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int i = lane + 32 * (u0 + q);
+      vc[q] = (i > c && i < m) ? v[i] : zero_<T>();
+    }
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int u = u0 + q;
+      const int i = lane + 32 * u;
+      if (i == c) w0 += x[u];
+      else if ((q & 3) == 0) fma_(w0, conj_(vc[q]), x[u]);
+      else if ((q & 3) == 1) fma_(w1, conj_(vc[q]), x[u]);
+      else if ((q & 3) == 2) fma_(w2, conj_(vc[q]), x[u]);
+      else fma_(w3, conj_(vc[q]), x[u]);
+    }
+  }
+  const T f = conj_(tau) * warp_sum((w0 + w1) + (w2 + w3));
+  const int c1 = c + 1;
+  R n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+  T a_l = zero_<T>();
+#pragma unroll
+  for (int u0 = 0; u0 < E; u0 += C) {
+    T vc[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int i = lane + 32 * (u0 + q);
+      vc[q] = (i > c && i < m) ? v[i] : zero_<T>();
+    }
+#pragma unroll
+    for (int q = 0; q < C; ++q) {
+      const int u = u0 + q;
+      const int i = lane + 32 * u;
+      x[u] = (i == c) ? x[u] - f : x[u] - f * vc[q];
+      const R a = (i > c1 && i < m) ? abs2_(x[u]) : R(0);
+      if ((q & 3) == 0) n0 += a; else if ((q & 3) == 1) n1 += a; else if ((q & 3) == 2) n2 += a; else n3 += a;
+      if (i == c1) a_l = x[u];
+    }
+  }
+  const R xn = warp_sum((n0 + n1) + (n2 + n3));
+  const T alpha = shfl_T(a_l, c1 & 31);
+  T t = zero_<T>();
+  T scal = one_<T>(), betaT = alpha;
+  if (!(xn == R(0) && imag_(alpha) == R(0))) {
+    const R beta = -copysign(sqrt(abs2_(alpha) + xn), real_(alpha));
+    betaT = from_real<T>(beta);
+    t = div_(betaT - alpha, betaT);
+    scal = div_(one_<T>(), alpha - betaT);
+  }
+#pragma unroll
+  for (int u = 0; u < E; ++u) {
+    const int i = lane + 32 * u;
+    if (i > c1 && i < m) x[u] = scal * x[u];
+    else if (i == c1) x[u] = betaT;
+    if (i < m) out[i] = x[u];
+  }
+  return t;
+}
+
 // x <- H_c^H x with v held in registers vv (v_c = 1 implied); used by the
 // Q formation kernel below
 template <typename T, int E>
@@ -282,6 +360,7 @@ __global__ void __launch_bounds__(kPanel * 32)
 qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, SyncWords* sw) {
   __shared__ T sv[2 * 32 * E];
   __shared__ T stau[2];
+  extern __shared__ __align__(16) unsigned char qr_panel_dyn[];  // kPanel staging rows of 32 * E
   const int64_t k = m < n ? m : n;
   const int mi = (int)m;  // rows <= 32 * E
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -296,56 +375,77 @@ qr_panel_kernel(T* Bt, int64_t m, int64_t n, int64_t ld, T* tau, int* flags, Syn
       x[u] = (i < mi) ? Bt[j * ld + i] : zero_<T>();
     }
   }
-  // reflectors of earlier panels, as they are published (read from L2)
+  // reflectors of earlier panels, as they are published: each is staged from
+  // L2 into this warp's shared-memory row (16 independent loads a lane in
+  // flight), then applied from there in two passes
   const int64_t cend = p0 < k ? p0 : k;
   if (has) {
+    T* stage = reinterpret_cast<T*>(qr_panel_dyn) + warp * (32 * E);
     for (int64_t c = 0; c < cend; ++c) {
       if (!warp_wait_flag(&flags[c], sw)) break;
-      apply_stream<T, E, true>(x, Bt + c * ld, ldcg(tau + c), (int)c, mi);
+      const T* src = Bt + c * ld;
+      const int ci = (int)c;
+      constexpr int CH = 16;
+#pragma unroll
+      for (int u0 = 0; u0 < E; u0 += CH) {
+        T vc[CH];
+#pragma unroll
+        for (int q = 0; q < CH && u0 + q < E; ++q) {
+          const int i = lane + 32 * (u0 + q);
+          vc[q] = (i > ci && i < mi) ? ldcg(src + i) : zero_<T>();
+        }
+#pragma unroll
+        for (int q = 0; q < CH && u0 + q < E; ++q) stage[lane + 32 * (u0 + q)] = vc[q];
+      }
+      __syncwarp();
+      apply_stream<T, E, false>(x, stage, ldcg(tau + c), ci, mi);
+      __syncwarp();
     }
   }
   __syncthreads();
   if (ld_volatile(&sw->err)) return;  // uniform: every warp sees the same error word after the barrier
   // this panel's reflectors.  Reflector c is written to shared memory buffer
-  // (c & 1) by its owner; after one CTA barrier the later columns apply it
-  // while the owner publishes it to global memory, and the owner of column
-  // c+1 builds reflector c+1 into the other buffer right after applying c
-  // (look-ahead), so each column costs one barrier.
+  // (c & 1) by its owner; after one barrier the later columns apply it, and
+  // the owner of column c+1 builds reflector c+1 into the other buffer right
+  // after applying c (look-ahead).  The owner of c is then done: it
+  // publishes c to global memory (stores, fence, flag) and leaves the loop,
+  // so the barrier of step w counts only warps w..kPanel-1 (a named barrier
+  // with a shrinking count) and no fence sits on the column chain.  The
+  // owner keeps its tau in a register (the shared slot is reused two steps
+  // later, possibly before a departed owner has read it).
   const int64_t nw = (k - p0) < kPanel ? (k - p0) : kPanel;
+  T my_tau = zero_<T>();
   if (nw > 0 && warp == 0) {
-    const T t = make_reflector_reg(x, (int)p0, mi);
+    my_tau = make_reflector_reg(x, (int)p0, mi);
 #pragma unroll
     for (int u = 0; u < E; ++u) {
       const int i = lane + 32 * u;
       if (i < mi) sv[i] = x[u];
     }
-    if (lane == 0) stau[0] = t;
+    if (lane == 0) stau[0] = my_tau;
   }
   for (int w = 0; w < nw; ++w) {
     const int64_t c = p0 + w;
     const int b = w & 1;
-    __syncthreads();
+    named_barrier(1, (kPanel - w) * 32);
     if (warp == w) {
 #pragma unroll
       for (int u = 0; u < E; ++u) {
         const int i = lane + 32 * u;
         if (i >= (int)c && i < mi) stcg(Bt + c * ld + i, x[u]);
       }
-      if (lane == 0) stcg(tau + c, stau[b]);
+      if (lane == 0) stcg(tau + c, my_tau);
       __threadfence();
       __syncwarp();
       if (lane == 0) atomicExch(&flags[c], 1);
-    } else if (has && warp > w) {
-      apply_stream<T, E, false>(x, sv + b * (32 * E), stau[b], (int)c, mi);
+      break;
+    }
+    if (has) {  // warp > w
       if (warp == w + 1 && w + 1 < nw) {
-        const T t = make_reflector_reg(x, (int)c + 1, mi);
-        T* nb = sv + (b ^ 1) * (32 * E);
-#pragma unroll
-        for (int u = 0; u < E; ++u) {
-          const int i = lane + 32 * u;
-          if (i < mi) nb[i] = x[u];
-        }
-        if (lane == 0) stau[b ^ 1] = t;
+        my_tau = apply_and_reflect<T, E>(x, sv + b * (32 * E), stau[b], (int)c, mi, sv + (b ^ 1) * (32 * E));
+        if (lane == 0) stau[b ^ 1] = my_tau;
+      } else {
+        apply_stream<T, E, false>(x, sv + b * (32 * E), stau[b], (int)c, mi);
       }
     }
   }
@@ -575,6 +675,27 @@ static int qr_gemm_splitk(int opA, int opB, int64_t M, int64_t N, int64_t K, con
   return launch_status(1);
 }
 
+// Dynamic shared memory of the panel kernel (kPanel staging rows of 32 * E
+// elements, up to 96 KB): the attribute is raised once per device.
+template <typename T, int E>
+static int ensure_panel_smem() {
+  constexpr size_t bytes = (size_t)kPanel * 32 * E * sizeof(T);
+  if constexpr (bytes <= 48 * 1024) {
+    return TNC_OK;
+  } else {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return TNC_ERR_CUDA;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load() & bit) return TNC_OK;
+    if (cudaFuncSetAttribute((const void*)qr_panel_kernel<T, E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes) != cudaSuccess)
+      return TNC_ERR_CUDA;
+    done.fetch_or(bit);
+    return TNC_OK;
+  }
+}
+
 // Unblocked dataflow factorisation of the m x n matrix whose transpose is at
 // Bt (row stride ld): reflectors in place, tau, per-column flags (zeroed by
 // the caller), errors in sw.  Returns the register width E of the panel
@@ -586,19 +707,25 @@ static int qr_dataflow(int64_t m, int64_t n, int64_t ld, T* Bt, T* tau, int* fla
   // register-resident panels when the column fits (E slots of 32 rows)
   const void* panel_fn = nullptr;
   int E = 0;
+  int attr_rc = TNC_OK;
   const int64_t slots = (m + 31) / 32;
   const int64_t maxE = sizeof(T) >= 16 ? 16 : 48;
-  if (slots <= 8) { panel_fn = (const void*)qr_panel_kernel<T, 8>; E = 8; }
-  else if (slots <= 16) { panel_fn = (const void*)qr_panel_kernel<T, 16>; E = 16; }
+  if (slots <= 8) { panel_fn = (const void*)qr_panel_kernel<T, 8>; E = 8; attr_rc = ensure_panel_smem<T, 8>(); }
+  else if (slots <= 16) { panel_fn = (const void*)qr_panel_kernel<T, 16>; E = 16; attr_rc = ensure_panel_smem<T, 16>(); }
   else if constexpr (sizeof(T) < 16) {
-    if (slots <= 32 && maxE >= 32) { panel_fn = (const void*)qr_panel_kernel<T, 32>; E = 32; }
-    else if (slots <= 48 && maxE >= 48) { panel_fn = (const void*)qr_panel_kernel<T, 48>; E = 48; }
+    if (slots <= 32 && maxE >= 32) {
+      panel_fn = (const void*)qr_panel_kernel<T, 32>; E = 32; attr_rc = ensure_panel_smem<T, 32>();
+    } else if (slots <= 48 && maxE >= 48) {
+      panel_fn = (const void*)qr_panel_kernel<T, 48>; E = 48; attr_rc = ensure_panel_smem<T, 48>();
+    }
   }
+  if (attr_rc) return attr_rc;
   if (panel_fn != nullptr) {
     const int64_t want = (n + kPanel - 1) / kPanel;
-    const int cap = coop_capacity(panel_fn, kPanel * 32, 0);
+    const size_t dyn = (size_t)kPanel * 32 * E * sizeof(T);
+    const int cap = coop_capacity(panel_fn, kPanel * 32, dyn);
     if (cap > 0 && want <= cap) {
-      if (cudaLaunchCooperativeKernel(panel_fn, dim3((unsigned)want), dim3(kPanel * 32), args, 0, st) != cudaSuccess)
+      if (cudaLaunchCooperativeKernel(panel_fn, dim3((unsigned)want), dim3(kPanel * 32), args, dyn, st) != cudaSuccess)
         return TNC_ERR_CUDA;
       *E_used = E;
       return launch_status(1);

@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import math
 import threading
+import time
 
 import numpy as np
 import torch
@@ -339,6 +340,63 @@ def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0
     return P
 
 
+def apply_compress_native(sites, mpo, chi, threshold=1e-15, log_norm_in=0.0, stats=None, block_rows=0,
+                          profile=None):
+    """``apply_compress`` as one native call (``tnc_sweep_apply_compress``):
+    the same algorithm, rank rule and norm handling, with the whole sweep run
+    by the library so the calling thread stays out of the interpreter (and
+    off its lock) until the sweep ends.  Sites and MPO as for
+    ``apply_compress``; returns the compressed sites (compact copies; the
+    sweep's workspace is released), ``stats.log_norm`` / ``stats.bonds`` /
+    ``stats.norm_folded`` when ``stats`` is given.  ``profile``: a ctypes
+    array of 9 doubles accumulating per-op CUDA-event time, calls and
+    algorithmic flops (QR, R-only QR, Jacobi), or None."""
+    import ctypes as C
+    N = len(sites)
+    dt = sites[0].dtype
+    sites = [s.contiguous() for s in sites]
+    mpo = [_ops.cast(w, dt).contiguous() for w in mpo]
+    d = int(sites[0].shape[0])
+    bonds = [int(sites[0].shape[1])] + [int(s.shape[2]) for s in sites]
+    mbonds = [int(mpo[0].shape[2])] + [int(w.shape[3]) for w in mpo]
+    b_arr = (C.c_int64 * (N + 1))(*bonds)
+    m_arr = (C.c_int64 * (N + 1))(*mbonds)
+    code = _ops.code(dt)
+    sz = C.c_size_t()
+    L.check("tnc_sweep_workspace_size",
+            L.lib().tnc_sweep_workspace_size(code, N, d, b_arr, m_arr, C.byref(sz)))
+    ws = torch.empty(int(sz.value), dtype=torch.uint8, device=sites[0].device)
+    s_arr = (C.c_void_p * N)(*[s.data_ptr() for s in sites])
+    w_arr = (C.c_void_p * N)(*[w.data_ptr() for w in mpo])
+    out_b = (C.c_int64 * (N + 1))()
+    out_o = (C.c_int64 * N)()
+    lnorm = C.c_double(float(log_norm_in))
+    folded = C.c_int(0)
+    st = L.lib().tnc_sweep_apply_compress(code, N, d, s_arr, b_arr, w_arr, m_arr, int(chi or 0), float(threshold),
+                                          int(block_rows), C.c_void_p(ws.data_ptr()), sz.value, out_b, out_o,
+                                          C.byref(lnorm), C.byref(folded), profile,
+                                          C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if st == L.ERR_ARG:
+        raise ValueError("zero state in the sweep (or bad arguments)")
+    if st == L.ERR_NONFINITE:
+        raise ValueError("array must not contain infs or NaNs")
+    if st == L.ERR_NOT_CONVERGED:
+        raise _ops.LinAlgError("SVD did not converge")
+    L.check("tnc_sweep_apply_compress", st)
+    es = torch.empty(0, dtype=dt).element_size()
+    out = []
+    for i in range(N):
+        n = d * out_b[i] * out_b[i + 1]
+        view = ws[out_o[i]: out_o[i] + n * es].view(dt).view(d, out_b[i], out_b[i + 1])
+        out.append(view.clone())
+    if stats is not None:
+        stats.bonds = list(out_b)[1:N]
+        stats.log_norm = lnorm.value
+        stats.norm_folded = bool(folded.value)
+        stats.norm = float(np.exp(lnorm.value)) if abs(lnorm.value) < 700 else float("inf")
+    return out
+
+
 def compress(sites, chi, threshold=1e-15, stats=None, log_norm_in=0.0, fold_norm=True):
     """``MatrixProductState.svd_compress(chi, threshold)`` on (phys, left,
     right) device sites (no MPO).  Returns (sites, log_norm): the state is
@@ -385,6 +443,56 @@ def run_batch(jobs, streams=None):
         if e is not None:
             raise e
     for s in streams:
+        cur.wait_stream(s)
+    return out
+
+
+def run_queue(jobs, workers, streams=None, stagger=0.0):
+    """Continuous batching: ``workers`` host threads, each on its own CUDA
+    stream, take callables from one shared queue until it is empty, so an
+    instance that finishes early picks up the next one instead of waiting
+    for the slowest of a fixed batch (instances in different phases -- QR
+    sweep, SVD sweep -- then share the GPU).  ``stagger`` (seconds): worker
+    w takes its first job w * stagger late, so identical instances do not
+    run their phases in lockstep.  Returns the results in job order."""
+    n = len(jobs)
+    workers = max(1, min(workers, n)) if n else 0
+    if streams is None:
+        streams = [torch.cuda.Stream() for _ in range(workers)]
+    out = [None] * n
+    errs = []
+    nxt = [0]
+    lock = threading.Lock()
+    dev = torch.cuda.current_device()
+    cur = torch.cuda.current_stream()
+
+    def work(w):
+        try:
+            torch.cuda.set_device(dev)
+            st = streams[w % len(streams)]
+            st.wait_stream(cur)
+            if stagger > 0 and w:
+                time.sleep(w * stagger)
+            with torch.cuda.stream(st):
+                while True:
+                    with lock:
+                        if errs or nxt[0] >= n:
+                            return
+                        i = nxt[0]
+                        nxt[0] += 1
+                    out[i] = jobs[i]()
+        except BaseException as e:  # surfaced below
+            with lock:
+                errs.append(e)
+
+    threads = [threading.Thread(target=work, args=(w,)) for w in range(workers)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errs:
+        raise errs[0]
+    for s in streams[:workers]:
         cur.wait_stream(s)
     return out
 
