@@ -39,7 +39,7 @@ N_SITES, PHYS, MPO_D, CHI = 64, 2, 3, 256
 # admission stagger of the work queue (seconds between workers' first jobs):
 # identical instances started together run their QR and SVD phases in
 # lockstep and contend for the same resources at the same time
-STAGGER = 0.025
+STAGGER = 0.02
 METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, complex128)"
 # dram bytes (read + write) per call of the dominant native op at the
 # workload's bulk shape (the Jacobi kernel of tnc_svd_rows on the 512 x 512
@@ -58,7 +58,7 @@ def parse():
     p.add_argument("--chi", type=int, default=CHI)
     p.add_argument("--cpu-sample-sites", type=int, default=28)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--batch", type=int, default=8, help="independent instances per GPU")
+    p.add_argument("--batch", type=int, default=12, help="independent instances per GPU")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 drop-in comparison")
     p.add_argument("--micro", default=None,
@@ -424,7 +424,8 @@ def run_ours(args):
                        "scheduling": "K steps x %d sweeps as one work queue on %d CUDA streams (continuous "
                                      "batching), workers admitted %d ms apart, each sweep one native call"
                                      % (B, B, int(STAGGER * 1e3)),
-                       "l2": "inputs larger than L2 (%d MPS of 134 MB in, 1.2 GB applied each)" % B},
+                       "l2": "inputs larger than L2 (%d MPS of 67 MB complex64 on the device, 0.6 GB applied "
+                             "each)" % B},
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d // 1,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
