@@ -195,6 +195,36 @@ def test_native_sweep_real_and_batched(gpu):
         assert 1 - O.fidelity(O.apply_compress_sweep(b, mpo, chi), got) < 1e-6
 
 
+@pytest.mark.parametrize("d,chi,cut,dt", [(3, 20, 10, np.float32), (4, 12, 40, np.complex64), (2, 16, 8, np.float64)])
+def test_native_sweep_shapes(gpu, d, chi, cut, dt):
+    """The native sweep on other physical dimensions and dtypes (the uneven
+    batch's shapes), with chi below (truncating) and above (keeping every
+    direction) the applied bonds, against the oracle's svd_compress."""
+    from tncontract_gb300 import engine as E
+    N = 10
+    cplx = np.iscomplexobj(np.zeros(0, dt))
+    sites = O.random_mps(3, N, d, chi, np.complex128 if cplx else np.float64, normalise=True)
+    ident = [np.eye(d).reshape(d, d, 1, 1) for _ in range(N)]
+    tdt = {np.float32: torch.float32, np.complex64: torch.complex64, np.float64: torch.float64}[dt]
+    bal, ln = E.balance(sites)
+    st = E.SweepStats()
+    out = E.apply_compress_native(E.to_sites(bal, tdt), E.to_sites(ident, tdt), cut, log_norm_in=ln, stats=st)
+    got = [o.cpu().numpy().astype(np.complex128) for o in out]
+    ref = O.svd_compress_method(O.left_canonical_form_mps(sites), cut)
+    tol = 1e-10 if dt == np.float64 else 1e-6
+    assert 1 - O.fidelity(ref, got) < tol
+    assert [a.shape[2] for a in got[:-1]] == [a.shape[2] for a in ref[:-1]]
+    assert max(a.shape[2] for a in got) <= cut
+
+
+def test_native_sweep_zero_state(gpu):
+    from tncontract_gb300 import engine as E
+    sites = [np.zeros((2, 1, 4)), np.zeros((2, 4, 4)), np.zeros((2, 4, 1))]
+    ident = [np.eye(2).reshape(2, 2, 1, 1) for _ in range(3)]
+    with pytest.raises(ValueError):
+        E.apply_compress_native(E.to_sites(sites, torch.float64), E.to_sites(ident, torch.float64), 4)
+
+
 def test_engine_run_queue(gpu):
     """Continuous batching: 6 sweep jobs on 3 worker streams give the same
     results as the oracle, in job order."""
