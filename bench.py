@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--batch", type=int, default=12, help="independent instances per GPU")
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 drop-in comparison")
+    p.add_argument("--workload", default="tfim", choices=["tfim", "uneven"],
+                   help="tfim: the headline sweep; uneven: the uneven batch of independent MPS")
+    p.add_argument("--instances", type=int, default=512, help="instances of the uneven batch")
     p.add_argument("--micro", default=None,
                    help="time one native op instead: svd:MxN:DT, qr:MxN:DT or gemm:MxNxK:DT "
                         "(DT in f32,f64,c64,c128); used for kernel profiling")
@@ -448,10 +451,103 @@ def run_ours(args):
     return 0
 
 
+def run_uneven(args):
+    """The uneven batch: ``--instances`` independent random MPS (seed 1: N in
+    [16, 128], d in {2, 3, 4}, chi in [16, 256], float32 / complex64
+    alternating, ``workloads.config3_specs``), each left-canonised, svd-
+    compressed to chi // 2 (QR sweep + truncating SVD sweep, one native call
+    with an identity MPO) and its norm evaluated.  Inputs are generated on
+    the device from per-instance seeds (Gaussian entries, each site scaled to
+    unit expected norm) before the timed region; the jobs run heaviest first
+    on a work queue of ``--batch`` streams.  A sample of instances is checked
+    against the oracle (fidelity error) and timed on the host cores as the
+    CPU baseline, scaled to the whole batch by the flop ratio."""
+    import numpy as np
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import __graft_entry__
+    __graft_entry__.build()
+    from tncontract_gb300 import _ops
+    from tncontract_gb300 import engine as E
+    from tncontract_gb300 import workloads as W
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    specs = W.config3_specs(1, args.instances)
+    tdt = {np.float32: torch.float32, np.complex64: torch.complex64}
+    inputs, idents = [], {}
+    for (N, d, chi, dt, seed) in specs:
+        td = tdt[dt]
+        bonds = [1] + [chi] * (N - 1) + [1]
+        sites = []
+        for i in range(N):
+            a = _ops.fill_gaussian((d, bonds[i], bonds[i + 1]), td, seed * 1000 + i)
+            n = a.numel() * (2 if td == torch.complex64 else 1)
+            sites.append(_ops.scale(a, 1.0 / np.sqrt(n)))
+        inputs.append(sites)
+        if (d, td) not in idents:
+            idents[(d, td)] = _ops.to_device(np.eye(d).reshape(d, d, 1, 1), td)
+    torch.cuda.synchronize()
+    order = sorted(range(len(specs)), key=lambda i: -W.spec_flops(specs[i]))
+    results = [None] * len(specs)
+
+    def job(i):
+        def f():
+            N, d, chi, dt, _ = specs[i]
+            st = E.SweepStats()
+            out = E.apply_compress_native(inputs[i], [idents[(d, tdt[dt])]] * N, chi // 2, stats=st)
+            results[i] = (st.log_norm, st.bonds, out if i in sample else None)
+        return f
+
+    small = sorted(range(len(specs)), key=lambda i: W.spec_flops(specs[i]))
+    sample = set(small[:6] + small[len(small) // 4: len(small) // 4 + 2])
+    B = args.batch
+    streams = [torch.cuda.Stream() for _ in range(B)]
+    E.run_queue([job(i) for i in order[:B]], B, streams=streams, stagger=STAGGER)   # warm-up
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        torch.cuda.synchronize()
+        e0.record()
+        E.run_queue([job(i) for i in order], B, streams=streams, stagger=STAGGER)
+        e1.record()
+        torch.cuda.synchronize()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    # parity and CPU baseline on the sample
+    import tn_oracle as O
+    fid_err, cpu_s = 0.0, 0.0
+    for i in sorted(sample):
+        N, d, chi, dt, _ = specs[i]
+        host = [a.cpu().numpy().astype(np.complex128 if dt == np.complex64 else np.float64) for a in inputs[i]]
+        t0 = time.perf_counter()
+        ref = O.svd_compress_method(O.left_canonical_form_mps(host), chi // 2)
+        cpu_s += time.perf_counter() - t0
+        got = [o.cpu().numpy().astype(np.complex128) for o in results[i][2]]
+        fid_err = max(fid_err, 1 - O.fidelity(ref, got))
+    ratio = sum(W.spec_flops(specs[i]) for i in sample) / sum(W.spec_flops(sp) for sp in specs)
+    cpu_rate = len(specs) * ratio / cpu_s if cpu_s > 0 else None
+    line = {"metric": "uneven-batch instances/s (left-canonise + svd_compress to chi/2 + norm; N 16-128, "
+                      "d 2-4, chi 16-256)",
+            "value": len(specs) / elapsed, "unit": "instances/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": elapsed * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32/c64", "data": "synthetic (seeded Gaussian MPS generated on the device)",
+            "config": {"workload": "uneven_batch", "instances": len(specs), "seed": 1, "streams": B,
+                       "scheduling": "heaviest first on a work queue, workers admitted %d ms apart"
+                                     % int(STAGGER * 1e3)},
+            "fidelity_error_max_vs_oracle": fid_err, "oracle_sample": len(sample),
+            "clocks": clk.summary(),
+            "cpu_baseline": {"value": cpu_rate, "unit": "instances/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "%d instances of the batch through the oracle (left_canonical_form + "
+                                       "svd_compress), scaled by their flop share %.4f" % (len(sample), ratio)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.micro:
         return run_micro(args)
+    if args.workload == "uneven":
+        return run_uneven(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
