@@ -14,8 +14,8 @@ namespace tnc {
 constexpr long long kSpinLimit = 1LL << 24;
 
 struct SyncWords {
-  unsigned count;  // arrivals at the current barrier
-  unsigned gen;    // barrier generation
+  unsigned count;  // grid barrier arrivals; the top bit is the phase
+  unsigned gen;    // unused (keeps the layout of the zeroed words)
   int err;         // first error recorded by any CTA (0 = none)
   int pad;
 };
@@ -24,28 +24,30 @@ __device__ __forceinline__ int ld_volatile(const int* p) { return *(volatile con
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(volatile const unsigned*)p; }
 
 // All CTAs of the grid; returns false if any CTA recorded an error.
+// One atomic per CTA and barrier: CTA 0 adds 0x80000000 - (nblocks - 1), the
+// others 1, so the arrivals of one barrier add exactly 0x80000000 and flip the
+// top bit of `count` while leaving its low bits unchanged (partial sums stay
+// below the flip until the last arrival).  The value the atomic returns tells
+// each CTA the phase it waits to see flipped; `count` needs no reset.  A CTA
+// that records an error never arrives, so a completed barrier implies no error
+// before it; waiters poll the error word while they spin.
 __device__ __forceinline__ bool grid_barrier(SyncWords* sw, unsigned nblocks) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    unsigned g = ld_volatile(&sw->gen);
+    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (nblocks - 1u) : 1u;
     __threadfence();
-    unsigned prev = atomicAdd(&sw->count, 1u);
-    if (prev == nblocks - 1) {
-      atomicExch(&sw->count, 0u);
-      __threadfence();
-      atomicAdd(&sw->gen, 1u);
-    } else {
-      long long spins = 0;
-      while (ld_volatile(&sw->gen) == g) {
-        if (ld_volatile(&sw->err)) { ok = 0; break; }
-        if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
-        __nanosleep(64);
-      }
+    const unsigned old = atomicAdd(&sw->count, add);
+    // the CTA whose arrival flips the phase bit completed the barrier
+    const bool last = (((old + add) ^ old) & 0x80000000u) != 0;
+    long long spins = 0;
+    while (!last && ((ld_volatile(&sw->count) ^ old) & 0x80000000u) == 0) {
+      if (ld_volatile(&sw->err)) { ok = 0; break; }
+      if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
+      __nanosleep(32);
     }
     __threadfence();
-    if (ld_volatile(&sw->err)) ok = 0;
     ok_s = ok;
   }
   __syncthreads();

@@ -172,8 +172,17 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
   for (int64_t e = threadIdx.x; e < total; e += blockDim.x) stcg(W + row0 * L + e, s[e]);
 }
 
+// FP32 rows of up to 512 elements in 256-thread CTAs are held to 128 registers
+// so two CTAs fit on one SM: the kernel is latency-bound (8 warps, dependent
+// rotation steps), and concurrent factorisations on other streams fill the
+// second slot.  The bound costs a few spilled registers.
 template <typename T, int MAXE, int MAXT>
-__global__ void __launch_bounds__(MAXT)
+constexpr int jacobi_min_blocks() {
+  return (MAXT == 256 && MAXE <= 16 && sizeof(typename traits<T>::real) == 4) ? 2 : 1;
+}
+
+template <typename T, int MAXE, int MAXT>
+__global__ void __launch_bounds__(MAXT, jacobi_min_blocks<T, MAXE, MAXT>())
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
                     typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
