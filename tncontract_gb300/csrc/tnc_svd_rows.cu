@@ -18,10 +18,13 @@
 //              registers (warp i owns row i of P) and the rows of Q in shared
 //              memory, and rotates every (P_i, Q_j) pair in h steps (step s:
 //              warp i pairs with Q_{(i+s) mod h}).
-// Grid barriers separate phase 0 and the rounds: 2n/h per sweep instead of
-// n for a point ordering, and each rotation streams its rows through
-// registers and shared memory instead of L2.  One cooperative launch runs all
-// sweeps; barriers are bounded (tnc_persist.cuh).
+// A task of one step (phase 0 or a round) waits only for the tasks of the
+// previous step that wrote its two half-blocks (a step counter per
+// half-block); one grid barrier per sweep closes it for the convergence test.
+// That is 2n/h dependent steps per sweep instead of n for a point ordering,
+// and each rotation streams its rows through registers and shared memory
+// instead of L2.  One cooperative launch runs all sweeps; every wait is
+// bounded (tnc_persist.cuh).
 #include "tnc_persist.cuh"
 
 #include <atomic>
@@ -172,6 +175,43 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
   for (int64_t e = threadIdx.x; e < total; e += blockDim.x) stcg(W + row0 * L + e, s[e]);
 }
 
+// Step counters of the half-blocks: ver[b] = steps completed on half-block b
+// (phase 0 and the rounds, counted across sweeps).  The CTA that finished a
+// step on P and Q publishes after its rows are stored; the CTA that takes them
+// next waits for that, not for the whole grid.  Both are called by every
+// thread of the CTA.
+__device__ __forceinline__ void publish_steps(unsigned* ver, int64_t P, int64_t Q, unsigned value) {
+  __syncthreads();  // every thread's rows and norms stored
+  if (threadIdx.x == 0) {
+    __threadfence();
+    *(volatile unsigned*)(ver + P) = value;
+    if (Q != P) *(volatile unsigned*)(ver + Q) = value;
+  }
+}
+
+// Wait until P and Q have completed `target` steps; false on error / timeout.
+__device__ __forceinline__ bool wait_steps(const unsigned* ver, int64_t P, int64_t Q, unsigned target,
+                                           SyncWords* sw) {
+  __shared__ int ok_s;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    long long spins = 0;
+    for (;;) {
+      const unsigned a = ld_volatile(ver + P), b = ld_volatile(ver + Q);
+      if (a >= target && b >= target) break;
+      if (ld_volatile(&sw->err)) { ok = 0; break; }
+      if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
+      __nanosleep(32);
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  const int ok = ok_s;
+  __syncthreads();  // ok_s is free for the next wait
+  return ok != 0;
+}
+
 // FP32 rows of up to 512 elements in 256-thread CTAs are held to 128 registers
 // so two CTAs fit on one SM: the kernel is latency-bound (8 warps, dependent
 // rotation steps), and concurrent factorisations on other streams fill the
@@ -184,7 +224,7 @@ constexpr int jacobi_min_blocks() {
 template <typename T, int MAXE, int MAXT>
 __global__ void __launch_bounds__(MAXT, jacobi_min_blocks<T, MAXE, MAXT>())
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
-                    typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info) {
+                    typename traits<T>::real* Dn, unsigned* counters, unsigned* ver, SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sB = reinterpret_cast<T*>(smem_raw);
@@ -201,6 +241,10 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
   T x[MAXE];
   for (; sweep < max_sweeps; ++sweep) {
     unsigned rot = 0;
+    // step index of this sweep's phase 0; a sweep is nbp steps (phase 0 and
+    // nbp - 1 rounds).  The grid barrier that ends the previous sweep has
+    // ordered every earlier step, so phase 0 waits for nothing.
+    const unsigned g0 = (unsigned)sweep * (unsigned)nbp;
     // phase 0: pairs inside each half-block
     for (int64_t hb = blockIdx.x; hb < nb; hb += gridDim.x) {
       const int64_t row0 = hb * h;
@@ -224,16 +268,23 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
         __syncthreads();
       }
       rows_from_smem(W, row0, cnt, L, sB);
-      if (threadIdx.x < cnt) Dn[row0 + threadIdx.x] = sn[threadIdx.x];
-      __syncthreads();
+      if (threadIdx.x < cnt) stcg(Dn + row0 + threadIdx.x, sn[threadIdx.x]);
+      publish_steps(ver, hb, hb, g0 + 1u);
     }
-    if (!grid_barrier(sw, gridDim.x)) return;
-    // rounds over half-block pairs
+    // rounds over half-block pairs; a task waits only for the two tasks of
+    // the previous step that wrote its half-blocks
     for (int64_t r = 0; r < nbp - 1; ++r) {
+      const unsigned g = g0 + 1u + (unsigned)r;
       for (int64_t t = blockIdx.x; t < ntask; t += gridDim.x) {
         int64_t P, Q;
         circle_pair(nbp, r, t, P, Q);
-        if (P >= nb || Q >= nb) continue;  // uniform over the CTA
+        if (P >= nb || Q >= nb) {  // paired with the padding block: pass the real one on
+          const int64_t Pr = P < nb ? P : Q;
+          if (!wait_steps(ver, Pr, Pr, g, sw)) return;
+          publish_steps(ver, Pr, Pr, g + 1u);
+          continue;
+        }
+        if (!wait_steps(ver, P, Q, g, sw)) return;
         const int64_t rowA = P * h + warp;
         const bool hasA = rowA < nr;
         const int64_t q0 = Q * h;
@@ -266,9 +317,8 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
         }
         rows_from_smem(W, q0, cntB, L, sB);
         if (threadIdx.x < cntB) stcg(Dn + q0 + threadIdx.x, sn[threadIdx.x]);
-        __syncthreads();
+        publish_steps(ver, P, Q, g + 1u);
       }
-      if (!grid_barrier(sw, gridDim.x)) return;
     }
     if (lane == 0 && rot) atomicAdd(&counters[sweep], rot);
     if (!grid_barrier(sw, gridDim.x)) return;
@@ -343,7 +393,8 @@ static RowsLayout rows_layout(int64_t nr, size_t rs) {
   Ly.d = off; off = align256(off + (size_t)nr * rs);
   Ly.dn = off; off = align256(off + (size_t)nr * rs);
   Ly.frob2 = off; off = align256(off + sizeof(double));
-  Ly.counters = off; off = align256(off + kRowsMaxSweeps * sizeof(unsigned));
+  // sweep rotation counters, then one step counter per half-block (<= nr)
+  Ly.counters = off; off = align256(off + (kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned));
   Ly.sync = off; off = align256(off + sizeof(SyncWords));
   Ly.total = off;
   return Ly;
@@ -391,11 +442,12 @@ static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, 
   int64_t want = ntask;
   if (want < 1) want = 1;
   int grid = (int)(want < cap ? want : cap);
+  unsigned* ver = counters + kRowsMaxSweeps;
   int64_t nr_ = nr, L_ = L;
   int h_ = h, ms_ = ms;
   double tol_ = tol;
   void* args[] = {(void*)&W, (void*)&nr_, (void*)&L_, (void*)&h_, (void*)&ms_, (void*)&tol_,
-                  (void*)&frob2, (void*)&Dn, (void*)&counters, (void*)&sw, (void*)&info};
+                  (void*)&frob2, (void*)&Dn, (void*)&counters, (void*)&ver, (void*)&sw, (void*)&info};
   if (cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, st) != cudaSuccess) return TNC_ERR_CUDA;
   return TNC_OK;
 }
@@ -429,7 +481,8 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
                                                                                                       : TNC_ERR_CUDA;
   }
   if (s) return s;
-  if (cudaMemsetAsync(counters, 0, kRowsMaxSweeps * sizeof(unsigned), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(counters, 0, (kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned), st) != cudaSuccess)
+    return TNC_ERR_CUDA;
   if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(info, 0, 4 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
   int launched = 0;
