@@ -1,13 +1,18 @@
 // Batched GEMM on row-major operands with transpose / conjugate options
 // (the product inside np.tensordot, tncontract/tensor.py:735).
 //
-// CUDA-core tiled kernel: a 64x64 output tile per 256-thread CTA, 16-deep
-// K slices staged in shared memory (k-major so the inner loop reads 4
-// consecutive values of each operand), 4x4 register micro-tile per thread.
-// Tile loads are coalesced along whichever axis is contiguous in memory for
-// the requested op.  This is the FP64 / complex128 path (GB300 runs FP64 on
-// the CUDA cores) and the general fallback for small or odd shapes; FP32
-// class products large enough for the tensor cores go to the tcgen05 kernel.
+// CUDA-core tiled kernel: a 64x64 output tile per 256-thread CTA, 4x4
+// register micro-tile per thread, K in slices of BK staged in shared memory
+// k-major (so a thread reads its 4 consecutive values of each operand with
+// 16-byte loads).  Two shared-memory buffers: the next slice is fetched into
+// registers while the current one is multiplied, then stored to the other
+// buffer -- one CTA barrier per slice and the global-load latency hidden
+// behind the FMAs.  Whether an operand's contiguous axis is K (A: N/R,
+// B: T/C) or M/N (A: T/C, B: N/R) is a template parameter, so each tile load
+// is a coalesced, branch-free pattern.  This is the FP64 / complex128 path
+// (GB300 runs FP64 on the CUDA cores), the FP32-accurate path of the blocked
+// QR's products, and the general path for small or odd shapes; FP32-class
+// products that tolerate TF32-split accuracy can use the tcgen05 kernel.
 #include "tnc_common.cuh"
 
 namespace tnc {
@@ -15,20 +20,77 @@ namespace tnc {
 template <typename T>
 __device__ __forceinline__ T maybe_conj(T v, bool c) { return c ? conj_(v) : v; }
 
-template <typename T, int BM, int BN, int BK>
+// four consecutive elements of a 16-byte-aligned shared-memory row
+__device__ __forceinline__ void lds4(const float* p, float (&v)[4]) {
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&v)[4]) {
+  const double2 q0 = reinterpret_cast<const double2*>(p)[0], q1 = reinterpret_cast<const double2*>(p)[1];
+  v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+}
+__device__ __forceinline__ void lds4(const c64* p, c64 (&v)[4]) {
+  const float4 q0 = reinterpret_cast<const float4*>(p)[0], q1 = reinterpret_cast<const float4*>(p)[1];
+  v[0] = c64(q0.x, q0.y); v[1] = c64(q0.z, q0.w); v[2] = c64(q1.x, q1.y); v[3] = c64(q1.z, q1.w);
+}
+__device__ __forceinline__ void lds4(const c128* p, c128 (&v)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = p[i];
+}
+
+template <typename T>
+struct GemmTile {
+  static constexpr int BM = 64, BN = 64;
+  static constexpr int BK = sizeof(T) >= 16 ? 8 : 16;
+  static constexpr int PAD = sizeof(T) >= 16 ? 1 : 16 / (int)sizeof(T);  // rows stay 16-byte aligned
+  static constexpr int LD = BM + PAD;
+  static constexpr int PER = BM * BK / 256;  // tile elements each thread moves
+};
+
+// Fetch the BK-slice at k0 of a 64-row operand tile into registers.
+// KMAJOR: element (r, k) at X[r * ld + k] (lanes run along k);
+// else:   element (r, k) at X[k * ld + r] (lanes run along r).
+template <typename T, bool KMAJOR>
+__device__ __forceinline__ void tile_fetch(const T* __restrict__ X, int64_t ld, int64_t r0, int64_t R, int64_t k0,
+                                           int64_t K, T (&v)[GemmTile<T>::PER]) {
+  constexpr int BK = GemmTile<T>::BK;
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < GemmTile<T>::PER; ++j) {
+    int r, k;
+    if (KMAJOR) { k = t % BK; r = t / BK + (256 / BK) * j; }
+    else { r = t & 63; k = (t >> 6) + 4 * j; }
+    const int64_t gr = r0 + r, gk = k0 + k;
+    v[j] = (gr < R && gk < K) ? (KMAJOR ? X[gr * ld + gk] : X[gk * ld + gr]) : zero_<T>();
+  }
+}
+
+template <typename T, bool KMAJOR>
+__device__ __forceinline__ void tile_store(T* s, const T (&v)[GemmTile<T>::PER], bool cj) {
+  constexpr int BK = GemmTile<T>::BK, LD = GemmTile<T>::LD;
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < GemmTile<T>::PER; ++j) {
+    int r, k;
+    if (KMAJOR) { k = t % BK; r = t / BK + (256 / BK) * j; }
+    else { r = t & 63; k = (t >> 6) + 4 * j; }
+    s[k * LD + r] = maybe_conj(v[j], cj);
+  }
+}
+
+template <typename T, bool AK, bool BKM>
 __global__ void __launch_bounds__(256)
-gemm_simt_kernel(int opA, int opB, int64_t M, int64_t N, int64_t K, T alpha, const T* __restrict__ A,
-                 int64_t lda, int64_t sA, const T* __restrict__ B, int64_t ldb, int64_t sB, T beta,
-                 T* __restrict__ C, int64_t ldc, int64_t sC, int64_t batch) {
+gemm_simt_kernel(int64_t M, int64_t N, int64_t K, bool aC, bool bC, T alpha, const T* __restrict__ A, int64_t lda,
+                 int64_t sA, const T* __restrict__ B, int64_t ldb, int64_t sB, T beta, T* __restrict__ C,
+                 int64_t ldc, int64_t sC, int64_t batch) {
+  typedef GemmTile<T> G;
   constexpr int TM = 4, TN = 4;
-  constexpr int NT = 256;
-  __shared__ T As[BK][BM + 1];
-  __shared__ T Bs[BK][BN + 1];
+  __shared__ __align__(16) T As[2][G::BK * G::LD];
+  __shared__ __align__(16) T Bs[2][G::BK * G::LD];
   const int tid = threadIdx.x;
-  const int tx = tid % (BN / TN), ty = tid / (BN / TN);
-  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-  const bool aT = (opA == TNC_OP_T || opA == TNC_OP_C), aC = (opA == TNC_OP_C || opA == TNC_OP_R);
-  const bool bT = (opB == TNC_OP_T || opB == TNC_OP_C), bC = (opB == TNC_OP_C || opB == TNC_OP_R);
+  const int tx = tid % (G::BN / TN), ty = tid / (G::BN / TN);
+  const int64_t m0 = (int64_t)blockIdx.y * G::BM, n0 = (int64_t)blockIdx.x * G::BN;
+  const bool beta_zero = (abs2_(beta) == 0);
 
   for (int64_t bz = blockIdx.z; bz < batch; bz += gridDim.z) {
     const T* Ab = A + bz * sA;
@@ -40,48 +102,45 @@ gemm_simt_kernel(int opA, int opB, int64_t M, int64_t N, int64_t K, T alpha, con
 #pragma unroll
       for (int j = 0; j < TN; ++j) acc[i][j] = zero_<T>();
 
-    for (int64_t k0 = 0; k0 < K; k0 += BK) {
-#pragma unroll
-      for (int e = tid; e < BM * BK; e += NT) {
-        int m, k;
-        if (aT) { m = e % BM; k = e / BM; } else { k = e % BK; m = e / BK; }
-        int64_t gm = m0 + m, gk = k0 + k;
-        T v = zero_<T>();
-        if (gm < M && gk < K) v = aT ? Ab[gk * lda + gm] : Ab[gm * lda + gk];
-        As[k][m] = maybe_conj(v, aC);
+    T va[G::PER], vb[G::PER];
+    tile_fetch<T, AK>(Ab, lda, m0, M, 0, K, va);
+    tile_fetch<T, BKM>(Bb, ldb, n0, N, 0, K, vb);
+    tile_store<T, AK>(As[0], va, aC);
+    tile_store<T, BKM>(Bs[0], vb, bC);
+    __syncthreads();
+    int buf = 0;
+    for (int64_t k0 = 0; k0 < K; k0 += G::BK) {
+      const bool more = k0 + G::BK < K;
+      if (more) {
+        tile_fetch<T, AK>(Ab, lda, m0, M, k0 + G::BK, K, va);
+        tile_fetch<T, BKM>(Bb, ldb, n0, N, k0 + G::BK, K, vb);
       }
+      const T* as = As[buf];
+      const T* bs = Bs[buf];
 #pragma unroll
-      for (int e = tid; e < BN * BK; e += NT) {
-        int n, k;
-        if (bT) { k = e % BK; n = e / BK; } else { n = e % BN; k = e / BN; }
-        int64_t gn = n0 + n, gk = k0 + k;
-        T v = zero_<T>();
-        if (gn < N && gk < K) v = bT ? Bb[gn * ldb + gk] : Bb[gk * ldb + gn];
-        Bs[k][n] = maybe_conj(v, bC);
-      }
-      __syncthreads();
-#pragma unroll
-      for (int kk = 0; kk < BK; ++kk) {
+      for (int kk = 0; kk < G::BK; ++kk) {
         T a[TM], b[TN];
-#pragma unroll
-        for (int i = 0; i < TM; ++i) a[i] = As[kk][ty * TM + i];
-#pragma unroll
-        for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx * TN + j];
+        lds4(as + kk * G::LD + ty * TM, a);
+        lds4(bs + kk * G::LD + tx * TN, b);
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
           for (int j = 0; j < TN; ++j) fma_(acc[i][j], a[i], b[j]);
       }
+      if (more) {
+        tile_store<T, AK>(As[buf ^ 1], va, aC);
+        tile_store<T, BKM>(Bs[buf ^ 1], vb, bC);
+      }
       __syncthreads();
+      buf ^= 1;
     }
-    const bool beta_zero = (abs2_(beta) == 0);
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
-      int64_t gm = m0 + ty * TM + i;
+      const int64_t gm = m0 + ty * TM + i;
       if (gm >= M) continue;
 #pragma unroll
       for (int j = 0; j < TN; ++j) {
-        int64_t gn = n0 + tx * TN + j;
+        const int64_t gn = n0 + tx * TN + j;
         if (gn >= N) continue;
         T v = alpha * acc[i][j];
         if (!beta_zero) v += beta * Cb[gm * ldc + gn];
@@ -115,14 +174,23 @@ int gemm_launch(int opA, int opB, int64_t m, int64_t n, int64_t k, T alpha, cons
     gemm_scale_c<T><<<grid1d(m * n * batch, 256), 256, 0, st>>>(m, n, beta, C, ldc, sC, batch);
     return launch_status();
   }
-  constexpr int BM = 64, BN = 64, BK = (sizeof(T) >= 16 ? 8 : 16);
+  constexpr int BM = GemmTile<T>::BM, BN = GemmTile<T>::BN;
   int64_t gy = (m + BM - 1) / BM, gx = (n + BN - 1) / BN;
   if (gy > 65535) return TNC_ERR_ARG;
   if (gx > 0x7fffffff) return TNC_ERR_ARG;
   unsigned gz = (unsigned)(batch < 65535 ? batch : 65535);
   dim3 grid((unsigned)gx, (unsigned)gy, gz);
-  gemm_simt_kernel<T, BM, BN, BK><<<grid, 256, 0, st>>>(opA, opB, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
-                                                       ldc, sC, batch);
+  // A is K-contiguous for N / R, B for T / C
+  const bool aK = (opA == TNC_OP_N || opA == TNC_OP_R), bK = (opB == TNC_OP_T || opB == TNC_OP_C);
+  const bool aC = (opA == TNC_OP_C || opA == TNC_OP_R), bC = (opB == TNC_OP_C || opB == TNC_OP_R);
+#define TNC_GEMM_LAUNCH(AKV, BKV)                                                                              \
+  gemm_simt_kernel<T, AKV, BKV><<<grid, 256, 0, st>>>(m, n, k, aC, bC, alpha, A, lda, sA, B, ldb, sB, beta, C, \
+                                                      ldc, sC, batch)
+  if (aK && bK) TNC_GEMM_LAUNCH(true, true);
+  else if (aK) TNC_GEMM_LAUNCH(true, false);
+  else if (bK) TNC_GEMM_LAUNCH(false, true);
+  else TNC_GEMM_LAUNCH(false, false);
+#undef TNC_GEMM_LAUNCH
   return launch_status();
 }
 
