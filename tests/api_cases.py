@@ -181,3 +181,156 @@ def check_config2_small(tn, fid_tol=1e-10):
     assert f.bonddims() == m["c2s_f_bonds"]
     fs = sites_of(f)
     assert abs(O.fidelity(fs, ms) - float(np.real(g["c2s_fid_f_m"]))) < fid_tol
+
+
+def _mps_sites(net, phys=None):
+    """(phys, left, right) arrays of an MPS-like network's sites."""
+    phys = phys or net.phys_label
+    out = []
+    for t in net:
+        lab = t.labels
+        out.append(np.transpose(t.to_numpy(), [lab.index(phys), lab.index(net.left_label),
+                                                lab.index(net.right_label)]))
+    return out
+
+
+def _same_state(ref_sites, got_sites, tol):
+    """The two site lists describe the same state: fidelity and norm."""
+    import tn_oracle as O
+    nr, ng = O.mps_norm(ref_sites), O.mps_norm(got_sites)
+    assert abs(nr - ng) <= tol * nr, (nr, ng)
+    assert 1.0 - O.fidelity(ref_sites, got_sites) < tol
+
+
+def _lambdas(net):
+    return [np.diag(net[2 * i].to_numpy()) for i in range(net.nsites_physical + 1)]
+
+
+def _full_tensor(net, legs):
+    """Contract an open MPO / MPS chain on the host into one array with the
+    given per-site leg groups (e.g. [["physout", "physin"]] * n)."""
+    acc = None
+    out_legs = []
+    for t, group in zip(net, legs):
+        lab = list(t.labels)
+        a = np.transpose(t.to_numpy(), [lab.index(net.left_label)] + [lab.index(x) for x in group]
+                         + [lab.index(net.right_label)])
+        acc = a if acc is None else np.tensordot(acc, a, axes=([acc.ndim - 1], [0]))
+        out_legs += group
+    return acc.reshape(acc.shape[1:-1])
+
+
+def check_onedim_extras(tn, tol=1e-10):
+    """Gates, expectation values, reduced density matrices, variational
+    compression, the Gamma-Lambda canonical form, tensor -> MPS / MPO and the
+    onedim_utils constructors against the reference's fixtures.  States are
+    compared gauge-invariantly (fidelity, norm, Schmidt values, density
+    matrices, expectation values); constructor outputs exactly."""
+    g, m = load("onedim_extras")
+    oc = tn.onedim
+    sites6 = unpack(g, "x_psi")
+
+    def mps_of(sites):
+        return oc.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+
+    g2 = tn.Tensor(g["x_G2"], ["o1", "o2", "i1", "i2"])
+    g3 = tn.Tensor(g["x_G3"], ["o1", "o2", "o3", "i1", "i2", "i3"])
+    op1 = tn.Tensor(g["x_op1"], ["o", "i"])
+    # swap_gate
+    a = mps_of(sites6)
+    a.swap_gate(2)
+    assert a.bonddims() == m["x_swap_bonds"] and [t.labels for t in a] == m["x_swap_labels"]
+    _same_state(unpack(g, "x_swap"), _mps_sites(a), tol)
+    # apply_gate
+    for tag, gate, first, kw in [("x_ag2l", g2, 2, {}), ("x_ag2r", g2, 2, {"canonise": "right"}),
+                                 ("x_ag3c", g3, 1, {"chi": 3})]:
+        b = mps_of(sites6)
+        b.apply_gate(gate, first, **kw)
+        assert b.bonddims() == m[tag + "_bonds"], tag
+        assert [t.labels for t in b] == m[tag + "_labels"], tag
+        _same_state(unpack(g, tag), _mps_sites(b), tol)
+    # expval, ptrace
+    e = mps_of(sites6)
+    val = complex(e.expval(g2, 2).to_numpy().reshape(()))
+    assert abs(val - complex(g["x_expval"])) <= tol * max(abs(complex(g["x_expval"])), 1.0)
+    assert e.bonddims() == m["x_expval_bonds"]
+    f = mps_of(sites6)
+    rho = f.ptrace(1, 2)
+    assert rho.labels == m["x_ptrace_labels"] and close(rho.to_numpy(), g["x_ptrace"], tol)
+    # variational compression (iterative: looser bound)
+    p8 = mps_of(unpack(g, "x_psi8"))
+    v = p8.variational_compress(4, max_iter=20, tolerance=1e-8)
+    assert v.bonddims() == m["x_var_bonds"] and [t.labels for t in v] == m["x_var_labels"]
+    _same_state(unpack(g, "x_var"), _mps_sites(v), 1e-7)
+    v2 = oc.variational_compress_mps(mps_of(unpack(g, "x_psi8")), 3, max_iter=40, tolerance=1e-6)
+    _same_state(unpack(g, "x_var3"), _mps_sites(v2), 1e-5)
+    # canonical form
+    pc = oc.canonical_form_mps(mps_of(sites6))
+    assert [list(x) for x in pc.check_canonical_form(threshold=1e-10, print_output=False)] == m["x_can_check"]
+    assert pc.bonddims() == m["x_can_bonds"]
+    assert abs(pc.norm() - float(g["x_can_norm"])) <= tol
+    for lam, ref in zip(_lambdas(pc), unpack(g, "x_can_lam")):
+        assert close(lam, ref, tol)
+    val = complex(pc.expval(g2, 1).to_numpy().reshape(()))
+    assert abs(val - complex(g["x_can_expval"])) <= tol * max(abs(complex(g["x_can_expval"])), 1.0)
+    assert close(pc.ptrace(2).to_numpy(), g["x_can_ptrace"], tol)
+    pg = pc.copy()
+    pg.apply_gate(g2, 1, chi=3)
+    pg.apply_gate(op1, 3)
+    pg.swap_gate(2)
+    for lam, ref in zip(_lambdas(pg), unpack(g, "x_cang_lam")):
+        assert close(lam, ref, 1e-9)
+    _same_state(unpack(g, "x_cang_left"), _mps_sites(oc.canonical_to_left_canonical(pg)), 1e-9)
+    _same_state(unpack(g, "x_cang_right"), _mps_sites(oc.canonical_to_right_canonical(pg)), 1e-9)
+    pb = pc.copy()
+    pb.compress_bond(1, chi=2)
+    for lam, ref in zip(_lambdas(pb), unpack(g, "x_canb_lam")):
+        assert close(lam, ref, 1e-9)
+    lc = oc.left_canonical_to_canonical(oc.left_canonical_form_mps(mps_of(sites6)))
+    for lam, ref in zip(_lambdas(lc), unpack(g, "x_lcan_lam")):
+        assert close(lam, ref, tol)
+    # tensor -> MPS / MPO
+    T = g["x_T"]
+    mt = oc.tensor_to_mps(tn.Tensor(T, ["a", "b", "c", "d"]))
+    assert mt.bonddims() == m["x_t2m_bonds"]
+    assert close(_full_tensor(mt, [["phys"]] * 4), T, tol)
+    mc = oc.tensor_to_mps(tn.Tensor(T, ["a", "b", "c", "d"]), chi=2)
+    assert mc.bonddims() == m["x_t2mc_bonds"]
+    _same_state(unpack(g, "x_t2mc"), _mps_sites(mc), tol)
+    Top = g["x_Top"]
+    mo = oc.tensor_to_mpo(tn.Tensor(Top, ["o1", "o2", "o3", "i1", "i2", "i3"]))
+    assert mo.bonddims() == m["x_t2o_bonds"] and [t.labels for t in mo] == m["x_t2o_labels"]
+    full = _full_tensor(mo, [["physout", "physin"]] * 3)            # (o1, i1, o2, i2, o3, i3)
+    assert close(np.transpose(full, [0, 2, 4, 1, 3, 5]), Top, tol)
+    # onedim_utils
+    sz = np.diag([1.0, -1.0])
+    sx = np.array([[0.0, 1.0], [1.0, 0.0]])
+    sy = np.array([[0.0, -1j], [1j, 0.0]])
+    ob = oc.onebody_sum_mpo([tn.matrices.sigmaz(), tn.matrices.sigmax(), tn.matrices.sigmay(), sz])
+    assert [t.labels for t in ob] == m["x_obs_labels"]
+    for t, ref in zip(ob, unpack(g, "x_obs")):
+        assert t.data.dtype == _torch_dtype(ref.dtype) and np.array_equal(t.to_numpy(), ref)
+    ev = oc.expvals_mps(mps_of(sites6), tn.Tensor(sz, ["o", "i"]))
+    assert close(ev, g["x_expvals"], tol)
+    ev2 = oc.expvals_mps(mps_of(sites6), [op1] * 3, sites=[0, 2, 5])
+    assert close(ev2, g["x_expvals_sites"], tol)
+    rhos = oc.ptrace_mps(mps_of(sites6))
+    assert rhos[0].labels == m["x_rhos_labels"]
+    for r, ref in zip(rhos, unpack(g, "x_rhos")):
+        assert close(r.to_numpy(), ref, tol)
+    for got, ref in [(oc.init_mps_allzero(4, 3), unpack(g, "x_zero")),
+                     (oc.init_mps_logical(3, [1, 0, 2], 3), unpack(g, "x_logical"))]:
+        for t, r in zip(got, ref):
+            assert np.array_equal(t.to_numpy(), r)
+    np.random.seed(7)
+    rnd = oc.init_mps_random(5, 2, 3)
+    assert [t.labels for t in rnd] == m["x_random_labels"]
+    for t, r in zip(rnd, unpack(g, "x_random")):
+        assert close(t.to_numpy(), r, 1e-12)
+    assert sx.shape == sy.shape
+
+
+def _torch_dtype(np_dtype):
+    import torch
+    return {np.dtype(np.float64): torch.float64, np.dtype(np.complex128): torch.complex128,
+            np.dtype(np.float32): torch.float32, np.dtype(np.complex64): torch.complex64}[np.dtype(np_dtype)]

@@ -3,7 +3,9 @@ library (andrewdarmawan/tncontract, pure Python on NumPy/SciPy) itself.
 
 Run from the repository root with the reference checkout importable:
 
-    python tests/golden/gen_golden.py /path/to/tncontract-checkout
+    python tests/golden/gen_golden.py /path/to/tncontract-checkout [--only=NAME ...]
+
+(``--only=onedim_extras`` regenerates one fixture file).
 
 The reference predates NumPy 2; two aliases it uses (``np.product``,
 ``np.float``) are restored at run time before it is imported.  The checkout is
@@ -245,21 +247,155 @@ def gen_peps(tn, store, meta, L, D, d, chi, tag, seed=2):
         store[tag + "_exact"] = np.array(float(np.real(ex.data)))
 
 
+def site_list(net, tn):
+    """Sites of an MPS-like network as (phys, left, right) arrays; networks
+    whose sites lack the physical leg (the Lambda sites of the canonical
+    form) are stored as (left, right) matrices."""
+    out = []
+    for t in net:
+        lab = list(t.labels)
+        if net.phys_label in lab:
+            perm = [lab.index(net.phys_label), lab.index(net.left_label), lab.index(net.right_label)]
+        else:
+            perm = [lab.index(net.left_label), lab.index(net.right_label)]
+        out.append(np.ascontiguousarray(np.transpose(t.data, perm)))
+    return out
+
+
+def gen_onedim_extras(tn, store, meta):
+    """Gates, expectation values, reduced density matrices, variational
+    compression, the Gamma-Lambda canonical form and its converters,
+    tensor -> MPS / MPO splits and the onedim_utils constructors
+    (onedim_core.py:95-127, 486-1327, 1448-1479, 1711-1928;
+    onedim_utils.py)."""
+    oc = tn.onedim
+    rng = np.random.default_rng(21)
+
+    def cgauss(*shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+    def mps_of(sites):
+        return oc.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+
+    sites6 = O.random_mps(5, 6, 2, 4, np.complex128, normalise=True)
+    pack_list("x_psi", sites6, store)
+    G2 = cgauss(2, 2, 2, 2)
+    G3 = cgauss(2, 2, 2, 2, 2, 2)
+    op1 = cgauss(2, 2)
+    store["x_G2"], store["x_G3"], store["x_op1"] = G2, G3, op1
+    g2 = tn.Tensor(G2, ["o1", "o2", "i1", "i2"])
+    g3 = tn.Tensor(G3, ["o1", "o2", "o3", "i1", "i2", "i3"])
+    # swap_gate (onedim_core.py:95-127)
+    a = mps_of(sites6)
+    a.swap_gate(2)
+    pack_list("x_swap", site_list(a, tn), store)
+    meta["x_swap_bonds"] = [int(x) for x in a.bonddims()]
+    meta["x_swap_labels"] = [list(t.labels) for t in a]
+    # apply_gate (onedim_core.py:662-739)
+    for tag, gate, first, kw in [("x_ag2l", g2, 2, {}), ("x_ag2r", g2, 2, {"canonise": "right"}),
+                                 ("x_ag3c", g3, 1, {"chi": 3})]:
+        b = mps_of(sites6)
+        b.apply_gate(gate, first, **kw)
+        pack_list(tag, site_list(b, tn), store)
+        meta[tag + "_bonds"] = [int(x) for x in b.bonddims()]
+        meta[tag + "_labels"] = [list(t.labels) for t in b]
+    # expval and ptrace (onedim_core.py:741-877)
+    e = mps_of(sites6)
+    store["x_expval"] = np.asarray(e.expval(g2, 2).data)
+    meta["x_expval_bonds"] = [int(x) for x in e.bonddims()]
+    f = mps_of(sites6)
+    rho = f.ptrace(1, 2)
+    store["x_ptrace"] = rho.data
+    meta["x_ptrace_labels"] = list(rho.labels)
+    # variational compression (onedim_core.py:486-631, 1476-1479)
+    sites8 = O.random_mps(6, 8, 2, 8, np.complex128, normalise=True)
+    pack_list("x_psi8", sites8, store)
+    p8 = mps_of(sites8)
+    v = p8.variational_compress(4, max_iter=20, tolerance=1e-8)
+    pack_list("x_var", site_list(v, tn), store)
+    meta["x_var_bonds"] = [int(x) for x in v.bonddims()]
+    meta["x_var_labels"] = [list(t.labels) for t in v]
+    store["x_var_norm"] = np.array(v.norm())
+    v2 = oc.variational_compress_mps(mps_of(sites8), 3, max_iter=40, tolerance=1e-6)
+    pack_list("x_var3", site_list(v2, tn), store)
+    # canonical form (onedim_core.py:880-1327, 1448-1454, 1836-1928)
+    pc = oc.onedim_core.canonical_form_mps(mps_of(sites6))
+    meta["x_can_check"] = [list(map(int, x)) for x in pc.check_canonical_form(threshold=1e-10, print_output=False)]
+    meta["x_can_bonds"] = [int(x) for x in pc.bonddims()]
+    store["x_can_norm"] = np.array(pc.norm())
+    pack_list("x_can_lam", [np.diag(pc[2 * i].data) for i in range(pc.nsites_physical + 1)], store)
+    store["x_can_expval"] = np.asarray(pc.expval(g2, 1).data)
+    store["x_can_ptrace"] = pc.ptrace(2).data
+    pg = pc.copy()
+    pg.apply_gate(g2, 1, chi=3)
+    pg.apply_gate(tn.Tensor(op1, ["o", "i"]), 3)
+    pg.swap_gate(2)
+    pack_list("x_cang_lam", [np.diag(pg[2 * i].data) for i in range(pg.nsites_physical + 1)], store)
+    pack_list("x_cang_left", site_list(oc.canonical_to_left_canonical(pg), tn), store)
+    pack_list("x_cang_right", site_list(oc.canonical_to_right_canonical(pg), tn), store)
+    pb = pc.copy()
+    pb.compress_bond(1, chi=2)
+    pack_list("x_canb_lam", [np.diag(pb[2 * i].data) for i in range(pb.nsites_physical + 1)], store)
+    lc = oc.left_canonical_to_canonical(oc.left_canonical_form_mps(mps_of(sites6)))
+    pack_list("x_lcan_lam", [np.diag(lc[2 * i].data) for i in range(lc.nsites_physical + 1)], store)
+    # tensor -> MPS / MPO (onedim_core.py:1711-1833)
+    T = cgauss(2, 3, 2, 2)
+    store["x_T"] = T
+    m = oc.tensor_to_mps(tn.Tensor(T, ["a", "b", "c", "d"]))
+    meta["x_t2m_bonds"] = [int(x) for x in m.bonddims()]
+    pack_list("x_t2m", site_list(m, tn), store)
+    mc = oc.tensor_to_mps(tn.Tensor(T, ["a", "b", "c", "d"]), chi=2)
+    meta["x_t2mc_bonds"] = [int(x) for x in mc.bonddims()]
+    pack_list("x_t2mc", site_list(mc, tn), store)
+    Top = cgauss(2, 2, 2, 2, 2, 2)
+    store["x_Top"] = Top
+    mo = oc.tensor_to_mpo(tn.Tensor(Top, ["o1", "o2", "o3", "i1", "i2", "i3"]))
+    meta["x_t2o_bonds"] = [int(x) for x in mo.bonddims()]
+    meta["x_t2o_labels"] = [list(t.labels) for t in mo]
+    # onedim_utils
+    import tncontract.matrices as mats
+    terms = [mats.sigmaz(), mats.sigmax(), mats.sigmay(), mats.sigmaz()]
+    ob = tn.onedim.onebody_sum_mpo(terms)
+    pack_list("x_obs", [t.data for t in ob], store)
+    meta["x_obs_labels"] = [list(t.labels) for t in ob]
+    ev = tn.onedim.expvals_mps(mps_of(sites6), tn.Tensor(np.asarray(mats.sigmaz()), ["o", "i"]))
+    store["x_expvals"] = np.asarray(ev)
+    ev2 = tn.onedim.expvals_mps(mps_of(sites6), [tn.Tensor(op1, ["o", "i"])] * 3, sites=[0, 2, 5])
+    store["x_expvals_sites"] = np.asarray(ev2)
+    rhos = tn.onedim.ptrace_mps(mps_of(sites6))
+    pack_list("x_rhos", [r.data for r in rhos], store)
+    meta["x_rhos_labels"] = list(rhos[0].labels)
+    z = tn.onedim.init_mps_allzero(4, 3)
+    pack_list("x_zero", [t.data for t in z], store)
+    lg = tn.onedim.init_mps_logical(3, [1, 0, 2], 3)
+    pack_list("x_logical", [t.data for t in lg], store)
+    np.random.seed(7)
+    rnd = tn.onedim.init_mps_random(5, 2, 3)
+    pack_list("x_random", [t.data for t in rnd], store)
+    meta["x_random_labels"] = [list(t.labels) for t in rnd]
+
+
 def main():
-    ref_path = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
+    ref_path = args[0] if args else "/root/reference"
     tn = _ref(ref_path)
-    store, meta = {}, {}
-    gen_label_cases(tn, store, meta)
-    gen_fixture_10site(tn, ref_path, store, meta)
-    np.savez_compressed(os.path.join(HERE, "labels_and_fixture.npz"), **store)
-    with open(os.path.join(HERE, "labels_and_fixture.json"), "w") as f:
-        json.dump(meta, f, indent=1)
+    if not only or "labels_and_fixture" in only:
+        store, meta = {}, {}
+        gen_label_cases(tn, store, meta)
+        gen_fixture_10site(tn, ref_path, store, meta)
+        np.savez_compressed(os.path.join(HERE, "labels_and_fixture.npz"), **store)
+        with open(os.path.join(HERE, "labels_and_fixture.json"), "w") as f:
+            json.dump(meta, f, indent=1)
     for fn, job in [("config1", lambda s, m: gen_config1(tn, s, m)),
                     ("config2_small", lambda s, m: gen_config2(tn, s, m, 12, 16, "c2s")),
                     ("config2_chi128", lambda s, m: gen_config2(tn, s, m, 64, 128, "c2")),
                     ("peps", lambda s, m: (gen_peps(tn, s, m, 4, 2, 2, 4, "p4"),
                                            gen_peps(tn, s, m, 8, 4, 2, 16, "p8c16"),
-                                           gen_peps(tn, s, m, 8, 4, 2, 64, "p8c64")))]:
+                                           gen_peps(tn, s, m, 8, 4, 2, 64, "p8c64"))),
+                    ("onedim_extras", lambda s, m: gen_onedim_extras(tn, s, m))]:
+        if only and fn not in only:
+            continue
         s, m = {}, {}
         t = time.perf_counter()
         job(s, m)

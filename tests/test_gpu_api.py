@@ -28,3 +28,7 @@ def test_config1_left_canonise_then_compress(gpu):
 
 def test_config2_small_apply_and_compress(gpu):
     K.check_config2_small(gpu)
+
+
+def test_onedim_extras(gpu):
+    K.check_onedim_extras(gpu)

@@ -41,6 +41,14 @@ def test_config2_small_host():
         K.check_config2_small(tn)
 
 
+def test_onedim_extras_host():
+    """Gates, expvals, ptrace, variational compression, the canonical form
+    and the onedim_utils constructors (host logic, CPU stand-in)."""
+    import tncontract_gb300 as tn
+    with cpu_ops():
+        K.check_onedim_extras(tn)
+
+
 def test_engine_rank_rules():
     """The engine's host-side rank rule equals the reference's (s/s_max >
     threshold, then at most chi) and is capped at the storage noise floor."""

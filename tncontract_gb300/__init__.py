@@ -15,6 +15,7 @@ from .label import *  # noqa: F401,F403
 from .tncon import con  # noqa: F401
 from . import tensor  # noqa: F401
 from . import onedim  # noqa: F401
+from . import matrices  # noqa: F401
 from . import twodim  # noqa: F401
 
 __version__ = "0.1.0"
