@@ -334,3 +334,20 @@ def _torch_dtype(np_dtype):
     import torch
     return {np.dtype(np.float64): torch.float64, np.dtype(np.complex128): torch.complex128,
             np.dtype(np.float32): torch.float32, np.dtype(np.complex64): torch.complex64}[np.dtype(np_dtype)]
+
+
+def check_con_cases(tn, rtol=1e-12):
+    """con on the reference's fixture networks: the default (cost-ordered)
+    plan and the argument order give the reference's labels and values,
+    including the orders for which the reference returns a merged tensor
+    twice."""
+    g, m = load("con_cases")
+    names = sorted({k[:-len("_out_labels")] for k in m if k.endswith("_out_labels")})
+    for name in names:
+        tensors = [tn.Tensor(g["%s_in%d" % (name, i)], labels)
+                   for i, labels in enumerate(m[name + "_in_labels"])]
+        pairs = [tuple(p) for p in m[name + "_pairs"]]
+        for order in ("cost", "argument"):
+            r = tn.con(tensors, pairs, order=order)
+            assert r.labels == m[name + "_out_labels"], (name, order, r.labels)
+            assert close(r.to_numpy(), g[name + "_out"], rtol), (name, order)

@@ -375,6 +375,56 @@ def gen_onedim_extras(tn, store, meta):
     meta["x_random_labels"] = [list(t.labels) for t in rnd]
 
 
+def con_networks(tn, rng):
+    """Networks for the con fixtures: (name, tensors, pairs); data drawn from
+    ``rng`` in a fixed order."""
+    def t(shape, labels, cplx=False):
+        a = rng.standard_normal(shape)
+        if cplx:
+            a = a + 1j * rng.standard_normal(shape)
+        return tn.Tensor(a, labels)
+    A, B = t((2, 6), ["a0", "a1"]), t((6, 6), ["b0", "b1"])
+    C, D = t((6, 6), ["c0", "c1"]), t((6, 2), ["d0", "d1"])
+    nets = [("chain_components", [A, B, C, D], [("a1", "b0"), ("c1", "d0"), ("b1", "c0")]),
+            ("chain_outer_first", [D, A, B, C], [("d1", "a0"), ("a1", "b0"), ("b1", "c0"), ("c1", "d0")])]
+    P, Q = t((3, 4, 5, 5), ["p0", "p1", "p2", "p3"], True), t((4, 6, 3), ["q0", "q1", "q2"], True)
+    R, S, V = t((6, 7), ["r0", "r1"]), t((7, 2), ["s0", "s1"]), t((9,), ["v0"])
+    nets.append(("ring_trace_multiedge", [P, Q, R, S, V],
+                 [("p2", "p3"), ("p1", "q0"), ("q1", "r0"), ("r1", "s0"), ("p0", "q2")]))
+    H = t((3, 4, 5), ["h0", "h1", "h2"])
+    leaves = [t((n,), ["l%d" % i]) for i, n in enumerate((3, 4, 5))]
+    nets.append(("star_scalar", [H] + leaves, [("h0", "l0"), ("h1", "l1"), ("h2", "l2")]))
+    # 2 x 3 grid: physical leg 2, bonds 3 between neighbours, 1 at the boundary
+    G = [t((2, 1 if r == 0 else 3, 3 if r == 0 else 1, 1 if c == 0 else 3, 3 if c < 2 else 1),
+           ["g%d%d%s" % (r, c, x) for x in "pudlr"]) for r in range(2) for c in range(3)]
+    pairs = [("g%d%dr" % (r, c), "g%d%dl" % (r, c + 1)) for r in range(2) for c in range(2)]
+    pairs += [("g0%dd" % c, "g1%du" % c) for c in range(3)]
+    nets.append(("grid_2x3", G, pairs))
+    # the same grid with the pairs in breadth-first order from the corner (every
+    # pair joins the growing component, so the reference contracts it exactly)
+    bfs = [("g00r", "g01l"), ("g00d", "g10u"), ("g01r", "g02l"), ("g01d", "g11u"), ("g10r", "g11l"),
+           ("g02d", "g12u"), ("g11r", "g12l")]
+    nets.append(("grid_2x3_bfs", G, bfs))
+    return nets
+
+
+def gen_con_cases(tn, store, meta):
+    """con (tncon.py:4-159) on networks that exercise its plan: a pair order
+    whose component bookkeeping returns a tensor twice (the reference's
+    result is kept as is), an order starting with an outer product, a ring
+    with a trace and a multi-edge plus a disconnected vector, a full
+    contraction to a scalar and a 2 x 3 grid with open legs."""
+    rng = np.random.default_rng(31)
+    for name, tensors, pairs in con_networks(tn, rng):
+        for i, x in enumerate(tensors):
+            store["%s_in%d" % (name, i)] = x.data
+        meta[name + "_in_labels"] = [list(x.labels) for x in tensors]
+        meta[name + "_pairs"] = [list(p) for p in pairs]
+        r = tn.con(tensors, pairs)
+        store[name + "_out"] = np.asarray(r.data)
+        meta[name + "_out_labels"] = list(r.labels)
+
+
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
@@ -393,7 +443,8 @@ def main():
                     ("peps", lambda s, m: (gen_peps(tn, s, m, 4, 2, 2, 4, "p4"),
                                            gen_peps(tn, s, m, 8, 4, 2, 16, "p8c16"),
                                            gen_peps(tn, s, m, 8, 4, 2, 64, "p8c64"))),
-                    ("onedim_extras", lambda s, m: gen_onedim_extras(tn, s, m))]:
+                    ("onedim_extras", lambda s, m: gen_onedim_extras(tn, s, m)),
+                    ("con_cases", lambda s, m: gen_con_cases(tn, s, m))]:
         if only and fn not in only:
             continue
         s, m = {}, {}

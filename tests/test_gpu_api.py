@@ -32,3 +32,7 @@ def test_config2_small_apply_and_compress(gpu):
 
 def test_onedim_extras(gpu):
     K.check_onedim_extras(gpu)
+
+
+def test_con_fixture_networks(gpu):
+    K.check_con_cases(gpu)
