@@ -328,6 +328,16 @@ def check_onedim_extras(tn, tol=1e-10):
     for t, r in zip(rnd, unpack(g, "x_random")):
         assert close(t.to_numpy(), r, 1e-12)
     assert sx.shape == sy.shape
+    # boundary-MPS PEPS contraction with variational compression
+    import tn_oracle as O
+    rows = O.random_peps(2, 4, 4, 2, 2)
+    peps = tn.twodim.SquareLatticePEPS(
+        [[tn.Tensor(a, ["phys", "up", "right", "down", "left"]) for a in r] for r in rows])
+    val = tn.twodim.inner_product_peps(peps, peps, exact_contract=False, chi=3,
+                                       compression_type="variational", max_iter=30, tolerance=1e-8)
+    val = complex(np.asarray(val.to_numpy() if hasattr(val, "to_numpy") else val).reshape(()))
+    ref = complex(g["x_peps_var"])
+    assert abs(val - ref) <= 1e-7 * abs(ref), (val, ref, complex(g["x_peps_exact"]))
 
 
 def _torch_dtype(np_dtype):

@@ -373,6 +373,16 @@ def gen_onedim_extras(tn, store, meta):
     rnd = tn.onedim.init_mps_random(5, 2, 3)
     pack_list("x_random", [t.data for t in rnd], store)
     meta["x_random_labels"] = [list(t.labels) for t in rnd]
+    # boundary-MPS PEPS contraction with variational compression
+    # (square_lattice.py:164-173): 4 x 4, D=2, d=2, chi=3
+    rows = O.random_peps(2, 4, 4, 2, 2)
+    peps = tn.twodim.SquareLatticePEPS(
+        [[tn.Tensor(a, ["phys", "up", "right", "down", "left"]) for a in r] for r in rows])
+    val = tn.twodim.inner_product_peps(peps, peps, exact_contract=False, chi=3,
+                                       compression_type="variational", max_iter=30, tolerance=1e-8)
+    store["x_peps_var"] = np.array(complex(np.asarray(val.data).reshape(())))
+    ex = tn.twodim.inner_product_peps(peps, peps, exact_contract=True)
+    store["x_peps_exact"] = np.array(complex(np.asarray(ex.data).reshape(())))
 
 
 def con_networks(tn, rng):

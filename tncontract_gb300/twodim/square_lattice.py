@@ -114,10 +114,13 @@ class SquareLatticeTensorNetwork():
 
     def mps_contract(self, chi, compression_type="svd", until_column=-1,
                      max_iter=10, tolerance=1e-14, return_all_columns=False):
-        """``square_lattice.py:130-203`` (SVD compression).  The running norm
-        is a host ``np.longdouble`` as in the reference."""
-        if compression_type != "svd":
-            raise NotImplementedError("only compression_type='svd' is provided")
+        """``square_lattice.py:130-203``: boundary-MPS contraction from the
+        left, each column's MPS compressed by ``svd_compress_mps`` (the norm
+        divided out of the first site) or ``variational_compress`` (out of the
+        last site).  The running norm is a host ``np.longdouble`` as in the
+        reference."""
+        if compression_type not in ("svd", "variational"):
+            raise ValueError("compression_type must be 'svd' or 'variational'")
         nrows, ncols = self.shape
         column_list = [] if return_all_columns else None
         norm = np.longdouble(1)
@@ -128,12 +131,20 @@ class SquareLatticeTensorNetwork():
             else:
                 column_mpo = column_to_mpo(self, col)
                 mps_to_compress = od.contract_mps_mpo(compressed_mps, column_mpo)
-            compressed_mps = od.svd_compress_mps(mps_to_compress, chi, normalise=False,
-                                                 threshold=tolerance)
-            mps_norm = compressed_mps.norm(canonical_form="right")
-            if mps_norm == 0.0:
-                return 0.0
-            compressed_mps[0].data = _ops.scale(compressed_mps[0].data, 1.0 / mps_norm)
+            if compression_type == "svd":
+                compressed_mps = od.svd_compress_mps(mps_to_compress, chi, normalise=False,
+                                                     threshold=tolerance)
+                mps_norm = compressed_mps.norm(canonical_form="right")
+                if mps_norm == 0.0:
+                    return 0.0
+                compressed_mps[0].data = _ops.scale(compressed_mps[0].data, 1.0 / mps_norm)
+            else:
+                compressed_mps = mps_to_compress.variational_compress(chi, max_iter=max_iter,
+                                                                      tolerance=tolerance)
+                mps_norm = compressed_mps.norm(canonical_form="left")
+                if mps_norm == 0.0:
+                    return 0.0
+                compressed_mps[-1].data = _ops.scale(compressed_mps[-1].data, 1.0 / mps_norm)
             norm *= mps_norm
             if return_all_columns:
                 mps_copy = compressed_mps.copy()
@@ -143,7 +154,8 @@ class SquareLatticeTensorNetwork():
                 if return_all_columns:
                     return column_list
                 compressed_mps.norm_factor = norm  # longdouble kept on the host
-                compressed_mps[0].data = _ops.scale(compressed_mps[0].data, float(norm))
+                site = 0 if compression_type == "svd" else -1
+                compressed_mps[site].data = _ops.scale(compressed_mps[site].data, float(norm))
                 return compressed_mps
         final_column_mps = column_to_mpo(self, ncols - 1)
         full = od.inner_product_mps(compressed_mps, final_column_mps,
