@@ -361,3 +361,50 @@ def check_con_cases(tn, rtol=1e-12):
             r = tn.con(tensors, pairs, order=order)
             assert r.labels == m[name + "_out_labels"], (name, order, r.labels)
             assert close(r.to_numpy(), g[name + "_out"], rtol), (name, order)
+
+
+def check_canonical_conversions(tn, decimal=10):
+    """The reference's own unit tests of the canonical-form converters
+    (tncontract/tests/test_canonical_form_mps_conversion.py:31-80) on the
+    same pickled 10-site MPS, with the same assertions and tolerances."""
+    from numpy import testing
+    g, m = load("labels_and_fixture")
+    sites = unpack(g, "fx_site")
+    oc = tn.onedim
+
+    def fresh():
+        return oc.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+
+    def ip(a, b):
+        return complex(np.asarray(oc.inner_product_mps(a, b).cpu()).reshape(()))
+
+    # test_right_and_left_canonical_to_canonical (the reference mutates one
+    # module-level MPS through both tests; the same sequence is replayed)
+    psi = fresh()
+    psi.svd_compress(threshold=1e-12, normalise=False)
+    psicr = oc.right_canonical_to_canonical(psi, threshold=1e-12)
+    testing.assert_almost_equal(psi.norm(), psicr.norm(), decimal=decimal)
+    l, r, n = psicr.check_canonical_form(threshold=1e-10, print_output=False)
+    assert (len(l), len(r), len(n)) == (0, 0, 1)
+    psi.left_canonise()
+    psicl = oc.left_canonical_to_canonical(psi, threshold=1e-12)
+    testing.assert_almost_equal(psi.norm(), psicr.norm(), decimal=decimal)
+    l, r, n = psicl.check_canonical_form(threshold=1e-10, print_output=False)
+    assert (len(l), len(r), len(n)) == (0, 0, 1)
+    testing.assert_almost_equal(ip(psicr, psicl), psi.norm() ** 2, decimal=decimal)
+    psi.svd_compress(threshold=1e-12, normalise=True)
+    psicr = oc.right_canonical_to_canonical(psi, threshold=1e-12)
+    assert [len(x) for x in psicr.check_canonical_form(threshold=1e-10, print_output=False)] == [0, 0, 0]
+    psi.left_canonise()
+    psicl = oc.left_canonical_to_canonical(psi, threshold=1e-12)
+    assert [len(x) for x in psicl.check_canonical_form(threshold=1e-10, print_output=False)] == [0, 0, 0]
+    testing.assert_almost_equal(ip(psicr, psicl), 1.0, decimal=decimal)
+    # test_right_canonical_to_canonical_and_back
+    psi.svd_compress(threshold=1e-12, normalise=True)
+    psic = oc.right_canonical_to_canonical(psi, threshold=1e-12)
+    psir = oc.canonical_to_right_canonical(psic)
+    psil = oc.canonical_to_left_canonical(psic)
+    testing.assert_almost_equal(ip(psi, psil), 1.0, decimal=decimal)
+    testing.assert_almost_equal(ip(psi, psir), 1.0, decimal=decimal)
+    assert psir.check_canonical_form(threshold=1e-10, print_output=False)[1] == 0
+    assert psil.check_canonical_form(threshold=1e-10, print_output=False)[0] == len(psi) - 1

@@ -36,3 +36,7 @@ def test_onedim_extras(gpu):
 
 def test_con_fixture_networks(gpu):
     K.check_con_cases(gpu)
+
+
+def test_canonical_conversions(gpu):
+    K.check_canonical_conversions(gpu)

@@ -49,6 +49,13 @@ def test_onedim_extras_host():
         K.check_onedim_extras(tn)
 
 
+def test_canonical_conversions_host():
+    """The reference's own converter tests, host logic on the CPU stand-in."""
+    import tncontract_gb300 as tn
+    with cpu_ops():
+        K.check_canonical_conversions(tn)
+
+
 def test_engine_rank_rules():
     """The engine's host-side rank rule equals the reference's (s/s_max >
     threshold, then at most chi) and is capped at the storage noise floor."""
