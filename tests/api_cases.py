@@ -408,3 +408,73 @@ def check_canonical_conversions(tn, decimal=10):
     testing.assert_almost_equal(ip(psi, psir), 1.0, decimal=decimal)
     assert psir.check_canonical_form(threshold=1e-10, print_output=False)[1] == 0
     assert psil.check_canonical_form(threshold=1e-10, print_output=False)[0] == len(psi) - 1
+
+
+def _raises_name(fn):
+    try:
+        fn()
+    except Exception as e:  # noqa: BLE001 -- compared with the reference's class name
+        return type(e).__name__
+    return None
+
+
+def check_onedim_edges(tn, tol=1e-10):
+    """Argument variants and error behaviour of the 1-D API against the
+    reference's fixtures (tests/golden/gen_golden.py: gen_onedim_edges)."""
+    g, m = load("onedim_edges")
+    oc = tn.onedim
+    sites = unpack(g, "e_psi")
+
+    def mps_of(s):
+        return oc.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in s])
+
+    gate = tn.Tensor(g["e_G"], ["a", "b", "c", "d"])
+    b = mps_of(sites)
+    b.apply_gate(gate, 1, gate_inputs=["a", "c"])
+    _same_state(unpack(g, "e_ag_in"), _mps_sites(b), tol)
+    c = mps_of(sites)
+    c.apply_gate(gate, 2, gate_outputs=["d", "b"])
+    _same_state(unpack(g, "e_ag_out"), _mps_sites(c), tol)
+    assert _raises_name(lambda: mps_of(sites).apply_gate(gate, 1, gate_inputs=["a"], gate_outputs=["b", "c"])) \
+        == m["e_ag_mismatch"]
+    e = mps_of(sites)
+    e.left_canonise(0, 2)
+    val = complex(e.expval(gate, 2, left_canonised_up_to=2, right_canonised_up_to=4).to_numpy().reshape(()))
+    ref = complex(g["e_expval_bounds"])
+    assert abs(val - ref) <= tol * max(abs(ref), 1.0)
+    assert e.bonddims() == m["e_expval_bounds_bonds"]
+    f = mps_of(sites)
+    rho = f.ptrace(3)
+    assert rho.labels == m["e_ptrace1_labels"] and close(rho.to_numpy(), g["e_ptrace1"], tol)
+    op = tn.Tensor(g["e_op"], ["o", "i"])
+    lc = oc.left_canonical_form_mps(mps_of(sites))
+    assert close(oc.expvals_mps(lc, op, canonised="left"), g["e_expvals_left"], tol)
+    rc = oc.right_canonical_form_mps(mps_of(sites))
+    assert close(oc.expvals_mps(rc, [op, op], sites=[1, 3], canonised="right"), g["e_expvals_right"], tol)
+    lc2 = oc.left_canonical_form_mps(mps_of(sites))
+    for r, ref in zip(oc.ptrace_mps(lc2, sites=[0, 4], canonised="left"), unpack(g, "e_rhos_left")):
+        assert close(r.to_numpy(), ref, tol)
+    mpo = oc.MatrixProductOperator([tn.Tensor(w, ["physout", "physin", "left", "right"]) for w in unpack(g, "e_mpo")])
+    mpo.swap_gate(1)
+    assert [t.labels for t in mpo] == m["e_mpo_swap_labels"] and mpo.bonddims() == m["e_mpo_swap_bonds"]
+    assert close(_full_tensor(mpo, [["physout", "physin"]] * 4), g["e_mpo_swap_full"], tol)
+    big = unpack(g, "e_big")
+    guess = oc.svd_compress_mps(mps_of(big), 3)
+    v = mps_of(big).variational_compress(3, max_iter=40, initial_guess=guess, tolerance=1e-8)
+    _same_state(unpack(g, "e_var_guess"), _mps_sites(v), 1e-6)
+    vn = mps_of(big).variational_compress(4, max_iter=40, tolerance=1e-8, normalise=True)
+    _same_state(unpack(g, "e_var_norm"), _mps_sites(vn), 1e-6)
+    assert abs(vn.norm() - complex(g["e_var_norm_value"]).real) < 1e-8
+    pc = oc.canonical_form_mps(mps_of(sites))
+    pc[3].data = pc[3].data * 1.5
+    assert [list(x) for x in pc.check_canonical_form(threshold=1e-10, print_output=False)] == m["e_can_bad"]
+    g3 = tn.Tensor(np.ones((2,) * 6), ["o1", "o2", "o3", "i1", "i2", "i3"])
+    assert _raises_name(lambda: pc.copy().apply_gate(g3, 0)) == m["e_can_gate3"]
+    assert _raises_name(lambda: pc.copy().compress_all()) == m["e_can_compress_all"]
+    T = tn.Tensor(g["e_Tmpo"], ["o1", "o2", "i1", "i2"])
+    mo = oc.tensor_to_mpo(T, physin_labels=["i1", "i2"])
+    assert [t.labels for t in mo] == m["e_t2o_in_labels"]
+    full = _full_tensor(mo, [["physout", "physin"]] * 2)             # (o1, i1, o2, i2)
+    assert close(np.transpose(full, [0, 2, 1, 3]), g["e_Tmpo"], tol)
+    assert _raises_name(lambda: oc.tensor_to_mpo(T, physout_labels=["o1"], physin_labels=["i1", "i2"])) \
+        == m["e_t2o_mismatch"]

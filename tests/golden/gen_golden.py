@@ -385,6 +385,96 @@ def gen_onedim_extras(tn, store, meta):
     store["x_peps_exact"] = np.array(complex(np.asarray(ex.data).reshape(())))
 
 
+def _raises(fn):
+    """Name of the exception ``fn()`` raises, or None."""
+    try:
+        fn()
+    except Exception as e:  # noqa: BLE001 -- the class name is the fixture
+        return type(e).__name__
+    return None
+
+
+def gen_onedim_edges(tn, store, meta):
+    """Argument variants and error behaviour of the 1-D API: explicit
+    gate_inputs / gate_outputs, partial canonisation bounds, left-canonical
+    inputs to expvals_mps / ptrace_mps, swap_gate on an MPO, variational
+    compression from an initial guess and normalised, non-canonical
+    Gamma-Lambda networks, and the errors each raises."""
+    oc = tn.onedim
+    rng = np.random.default_rng(41)
+
+    def cgauss(*shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+    def mps_of(sites):
+        return oc.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+
+    sites = O.random_mps(8, 5, 2, 3, np.complex128, normalise=True)
+    pack_list("e_psi", sites, store)
+    G = cgauss(2, 2, 2, 2)
+    store["e_G"] = G
+    g = tn.Tensor(G, ["a", "b", "c", "d"])
+    b = mps_of(sites)
+    b.apply_gate(g, 1, gate_inputs=["a", "c"])          # outputs: b, d
+    pack_list("e_ag_in", site_list(b, tn), store)
+    c = mps_of(sites)
+    c.apply_gate(g, 2, gate_outputs=["d", "b"])         # inputs: a, c
+    pack_list("e_ag_out", site_list(c, tn), store)
+    meta["e_ag_mismatch"] = _raises(lambda: mps_of(sites).apply_gate(g, 1, gate_inputs=["a"],
+                                                                    gate_outputs=["b", "c"]))
+    e = mps_of(sites)
+    e.left_canonise(0, 2)
+    store["e_expval_bounds"] = np.asarray(e.expval(g, 2, left_canonised_up_to=2, right_canonised_up_to=4).data)
+    meta["e_expval_bounds_bonds"] = [int(x) for x in e.bonddims()]
+    f = mps_of(sites)
+    rho = f.ptrace(3)
+    store["e_ptrace1"] = rho.data
+    meta["e_ptrace1_labels"] = list(rho.labels)
+    op = tn.Tensor(cgauss(2, 2), ["o", "i"])
+    store["e_op"] = op.data
+    lc = oc.left_canonical_form_mps(mps_of(sites))
+    store["e_expvals_left"] = np.asarray(oc.expvals_mps(lc, op, canonised="left"))
+    rc = oc.right_canonical_form_mps(mps_of(sites))
+    store["e_expvals_right"] = np.asarray(oc.expvals_mps(rc, [op, op], sites=[1, 3], canonised="right"))
+    lc2 = oc.left_canonical_form_mps(mps_of(sites))
+    rhos = oc.ptrace_mps(lc2, sites=[0, 4], canonised="left")
+    pack_list("e_rhos_left", [r.data for r in rhos], store)
+    # swap_gate on an MPO (all non-virtual legs move)
+    W = [cgauss(2, 2, 1 if i == 0 else 3, 1 if i == 3 else 3) for i in range(4)]
+    pack_list("e_mpo", W, store)
+    mpo = oc.MatrixProductOperator([tn.Tensor(w, ["physout", "physin", "left", "right"]) for w in W])
+    mpo.swap_gate(1)
+    meta["e_mpo_swap_labels"] = [list(t.labels) for t in mpo]
+    meta["e_mpo_swap_bonds"] = [int(x) for x in mpo.bonddims()]
+    Wfull = None
+    for t in mpo:
+        lab = list(t.labels)
+        a = np.transpose(t.data, [lab.index("left"), lab.index("physout"), lab.index("physin"), lab.index("right")])
+        Wfull = a if Wfull is None else np.tensordot(Wfull, a, axes=([Wfull.ndim - 1], [0]))
+    store["e_mpo_swap_full"] = Wfull.reshape(Wfull.shape[1:-1])
+    # variational compression from an initial guess, and normalised
+    big = O.random_mps(9, 6, 2, 6, np.complex128, normalise=False)
+    pack_list("e_big", big, store)
+    guess = oc.svd_compress_mps(mps_of(big), 3)
+    v = mps_of(big).variational_compress(3, max_iter=40, initial_guess=guess, tolerance=1e-8)
+    pack_list("e_var_guess", site_list(v, tn), store)
+    vn = mps_of(big).variational_compress(4, max_iter=40, tolerance=1e-8, normalise=True)
+    pack_list("e_var_norm", site_list(vn, tn), store)
+    store["e_var_norm_value"] = np.array(vn.norm())
+    # Gamma-Lambda: a perturbed network is not canonical; errors
+    pc = oc.onedim_core.canonical_form_mps(mps_of(sites))
+    pc[3].data = pc[3].data * 1.5
+    meta["e_can_bad"] = [list(map(int, x)) for x in pc.check_canonical_form(threshold=1e-10, print_output=False)]
+    g3 = tn.Tensor(cgauss(2, 2, 2, 2, 2, 2), ["o1", "o2", "o3", "i1", "i2", "i3"])
+    meta["e_can_gate3"] = _raises(lambda: pc.copy().apply_gate(g3, 0))
+    meta["e_can_compress_all"] = _raises(lambda: pc.copy().compress_all())
+    T = tn.Tensor(cgauss(2, 2, 2, 2), ["o1", "o2", "i1", "i2"])
+    store["e_Tmpo"] = T.data
+    mo = oc.tensor_to_mpo(T, physin_labels=["i1", "i2"])
+    meta["e_t2o_in_labels"] = [list(t.labels) for t in mo]
+    meta["e_t2o_mismatch"] = _raises(lambda: oc.tensor_to_mpo(T, physout_labels=["o1"], physin_labels=["i1", "i2"]))
+
+
 def con_networks(tn, rng):
     """Networks for the con fixtures: (name, tensors, pairs); data drawn from
     ``rng`` in a fixed order."""
@@ -454,7 +544,8 @@ def main():
                                            gen_peps(tn, s, m, 8, 4, 2, 16, "p8c16"),
                                            gen_peps(tn, s, m, 8, 4, 2, 64, "p8c64"))),
                     ("onedim_extras", lambda s, m: gen_onedim_extras(tn, s, m)),
-                    ("con_cases", lambda s, m: gen_con_cases(tn, s, m))]:
+                    ("con_cases", lambda s, m: gen_con_cases(tn, s, m)),
+                    ("onedim_edges", lambda s, m: gen_onedim_edges(tn, s, m))]:
         if only and fn not in only:
             continue
         s, m = {}, {}

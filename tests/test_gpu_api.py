@@ -40,3 +40,7 @@ def test_con_fixture_networks(gpu):
 
 def test_canonical_conversions(gpu):
     K.check_canonical_conversions(gpu)
+
+
+def test_onedim_edges(gpu):
+    K.check_onedim_edges(gpu)

@@ -49,6 +49,13 @@ def test_onedim_extras_host():
         K.check_onedim_extras(tn)
 
 
+def test_onedim_edges_host():
+    """Argument variants and errors of the 1-D API (CPU stand-in)."""
+    import tncontract_gb300 as tn
+    with cpu_ops():
+        K.check_onedim_edges(tn)
+
+
 def test_canonical_conversions_host():
     """The reference's own converter tests, host logic on the CPU stand-in."""
     import tncontract_gb300 as tn
