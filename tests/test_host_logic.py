@@ -63,6 +63,40 @@ def test_canonical_conversions_host():
         K.check_canonical_conversions(tn)
 
 
+def test_canonical_conversions_any_svd_phase_host():
+    """The converters keep the state when the SVD of the last (one-column)
+    site returns a V other than LAPACK's 1: the CPU stand-in's SVD is given a
+    different, equally valid gauge (U and V^H times a phase) there."""
+    import numpy as np
+    import torch
+    import tncontract_gb300 as tn
+    import tncontract_gb300._ops as ops
+    with cpu_ops():
+        base = ops.svd
+
+        def svd_other_gauge(M, *a, **k):
+            u, s, vh = base(M, *a, **k)
+            if M.shape[1] == 1:
+                ph = -1.0 if not M.is_complex() else complex(np.exp(0.7j))
+                u = u * (ph.conjugate() if isinstance(ph, complex) else ph)
+                vh = vh * ph
+            return u, s, vh
+        ops.svd = svd_other_gauge
+        try:
+            K.check_canonical_conversions(tn)
+            # complex input too (phase, not only a sign)
+            g, m = K.load("onedim_extras")
+            sites = [torch.from_numpy(a).numpy() for a in K.unpack(g, "x_psi")]
+            psi = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+            psi.right_canonise()
+            c = tn.onedim.right_canonical_to_canonical(psi)
+            back = tn.onedim.canonical_to_left_canonical(c)
+            ip = complex(tn.onedim.inner_product_mps(psi, back).reshape(()).item())
+            assert abs(ip - psi.norm() ** 2) < 1e-10
+        finally:
+            ops.svd = base
+
+
 def test_engine_rank_rules():
     """The engine's host-side rank rule equals the reference's (s/s_max >
     threshold, then at most chi) and is capped at the storage noise floor."""
@@ -96,3 +130,33 @@ def test_boundary_mps_engine_host():
         val, log10, _ = E.boundary_mps_contract(W.double_layer_arrays(rows), 16, precision="fp64")
         assert abs(log10 - m["p8c16_log10"]) < 1e-10
         assert np.isfinite(log10)
+
+
+def test_high_rank_permute_and_trace_plans():
+    """Permutations and traces of more axes than the kernels take are planned
+    on the host as fused steps of at most eight axes (numpy applies the
+    steps here; the device applies the same steps with tnc_permute)."""
+    import random
+    import numpy as np
+    from tncontract_gb300._ops import permutation_steps, fuse_trace, MAX_KERNEL_RANK
+    rng = random.Random(2)
+    for n in (3, 8, 9, 12, 16, 21):
+        for trial in range(20):
+            shape = [rng.choice([1, 2, 2, 3]) for _ in range(n)]
+            if np.prod(shape) > 300000:
+                continue
+            perm = list(range(n))
+            rng.shuffle(perm)
+            x = np.random.default_rng(trial).standard_normal(shape)
+            cur = x
+            for s, p in permutation_steps(shape, perm):
+                assert len(s) <= MAX_KERNEL_RANK
+                s, p = (s, p) if s else ([cur.size], [0])
+                cur = np.ascontiguousarray(np.transpose(cur.reshape(s), p))
+            assert np.array_equal(cur.reshape([shape[p] for p in perm]), np.transpose(x, perm))
+    for shape, a1, a2 in [([2, 3, 3, 2, 1, 2, 2, 3, 2, 2], 1, 7), ([2] * 4 + [3] + [2] * 5 + [3, 2], 10, 4)]:
+        x = np.random.default_rng(0).standard_normal(shape)
+        fs, b1, b2 = fuse_trace(shape, a1, a2)
+        got = np.trace(x.reshape(fs), axis1=b1, axis2=b2)
+        ref = np.trace(x, axis1=a1, axis2=a2)
+        assert np.allclose(got.reshape(ref.shape), ref)

@@ -148,9 +148,69 @@ def copy(t):
 # ------------------------------------------------------------------ movement
 
 
+MAX_KERNEL_RANK = 8  # tnc_permute / tnc_trace take at most this many axes
+
+
+def fuse_permutation(shape, perm):
+    """The same data movement on fewer axes: unit axes dropped, and input axes
+    that stay adjacent and in order in the output fused into one.  Returns
+    (fused input shape, fused permutation)."""
+    keep = [a for a in range(len(shape)) if shape[a] != 1]
+    index = {a: i for i, a in enumerate(keep)}
+    dims = [int(shape[a]) for a in keep]
+    p = [index[a] for a in perm if shape[a] != 1]
+    groups = []
+    for a in p:
+        if groups and groups[-1][-1] + 1 == a:
+            groups[-1].append(a)
+        else:
+            groups.append([a])
+    by_input = sorted(range(len(groups)), key=lambda g: groups[g][0])
+    fused_shape = [int(np.prod([dims[a] for a in groups[g]], dtype=np.int64)) for g in by_input]
+    position = {g: i for i, g in enumerate(by_input)}
+    return fused_shape, [position[g] for g in range(len(groups))]
+
+
+def permutation_steps(shape, perm, max_rank=MAX_KERNEL_RANK):
+    """Permutations of at most ``max_rank`` axes whose succession is
+    transpose(., perm): the fused permutation itself when it is small
+    enough, else single-axis moves (each a fused permutation of at most four
+    axes, one pass over the data) until the rest fits.  Each step is
+    (input shape, permutation) on the current contiguous layout."""
+    n = len(shape)
+    fs, fp = fuse_permutation(shape, perm)
+    if len(fs) <= max_rank:
+        return [(fs, fp)]
+    order = list(range(n))   # original axis at each current position
+    steps = []
+    for t in range(n):
+        current = [int(shape[a]) for a in order]
+        rest = [order.index(perm[k]) for k in range(n)]
+        fs, fp = fuse_permutation(current, rest)
+        if len(fs) <= max_rank:
+            steps.append((fs, fp))
+            return steps
+        pos = order.index(perm[t])
+        if pos == t:
+            continue
+        move = list(range(t)) + [pos] + list(range(t, pos)) + list(range(pos + 1, n))
+        steps.append(fuse_permutation(current, move))
+        order = [order[i] for i in move]
+    return steps
+
+
+def _permute_kernel(x, shape, perm, conj):
+    out = empty([shape[p] for p in perm], x.dtype)
+    _call("tnc_permute", code(x.dtype), _p(x), _p(out), len(shape),
+          _arr(C.c_int64, shape), _arr(C.c_int, perm), int(conj), _stream())
+    return out
+
+
 def permute(x, perm, conj=False):
     """Return transpose(x, perm) (optionally conjugated) as a new tensor;
-    ``x`` itself when the permutation is the identity and no conj is asked."""
+    ``x`` itself when the permutation is the identity and no conj is asked.
+    Tensors of more than ``MAX_KERNEL_RANK`` axes are moved in fused steps of
+    at most that many (``permutation_steps``)."""
     perm = [int(p) for p in perm]
     conj = bool(conj) and is_complex(x.dtype)
     if perm == list(range(x.dim())) and not conj:
@@ -160,12 +220,16 @@ def permute(x, perm, conj=False):
     moving = [p for p in perm if x.shape[p] != 1]
     if not conj and moving == sorted(moving):
         return x.reshape(shape)  # only unit axes move: a view suffices
-    out = empty(shape, x.dtype)
-    if out.numel() == 0:
-        return out
-    _call("tnc_permute", code(x.dtype), _p(x), _p(out), x.dim(),
-          _arr(C.c_int64, x.shape), _arr(C.c_int, perm), int(conj), _stream())
-    return out
+    if x.numel() == 0:
+        return empty(shape, x.dtype)
+    if x.dim() <= MAX_KERNEL_RANK:
+        return _permute_kernel(x, list(x.shape), perm, conj)
+    cur = x
+    for i, (s, p) in enumerate(permutation_steps(list(x.shape), perm)):
+        if not s:
+            s, p = [cur.numel()], [0]
+        cur = _permute_kernel(cur.reshape(s), s, p, conj and i == 0)
+    return cur.reshape(shape)
 
 
 def rollaxis(x, axis, start):
@@ -264,12 +328,28 @@ def scale_cols(A, d, mode=0):
 
 
 def trace(x, a1, a2):
+    """Trace over axes a1 and a2.  More than ``MAX_KERNEL_RANK`` axes: the
+    untouched axes before, between and after the pair are fused first (five
+    axes; the trace does not reorder them)."""
     x = x.contiguous()
     out = empty([s for i, s in enumerate(x.shape) if i not in (a1, a2)], x.dtype)
-    if out.numel():
-        _call("tnc_trace", code(x.dtype), x.dim(), _arr(C.c_int64, x.shape), int(a1), int(a2),
-              _p(x), _p(out), _stream())
+    if not out.numel():
+        return out
+    shape = list(x.shape)
+    if x.dim() > MAX_KERNEL_RANK:
+        shape, a1, a2 = fuse_trace(shape, a1, a2)
+    _call("tnc_trace", code(x.dtype), len(shape), _arr(C.c_int64, shape), int(a1), int(a2),
+          _p(x), _p(out), _stream())
     return out
+
+
+def fuse_trace(shape, a1, a2):
+    """(shape, a1, a2) of the same trace on five axes: the axes before,
+    between and after the traced pair fused."""
+    lo, hi = min(a1, a2), max(a1, a2)
+    prod = lambda d: int(np.prod(d, dtype=np.int64))
+    fused = [prod(shape[:lo]), int(shape[lo]), prod(shape[lo + 1:hi]), int(shape[hi]), prod(shape[hi + 1:])]
+    return (fused, 1, 3) if a1 < a2 else (fused, 3, 1)
 
 
 # ------------------------------------------------------------------ reductions

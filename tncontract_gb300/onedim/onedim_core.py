@@ -986,6 +986,12 @@ def right_canonical_to_canonical(mps, threshold=1e-14):
         V = tsr._new(V.data[0:k].contiguous(), V.labels)
         U.replace_label(svd_label + "in", R)
         V.replace_label(svd_label + "out", L)
+        if i == mps.nsites - 1 and V.data.numel() == 1:
+            # the last SVD has one column, so V is a 1x1 phase; LAPACK returns
+            # 1 there (the reference drops V), this library's SVD may not:
+            # keep the phase in the last Gamma so the state is unchanged
+            v = V.data.reshape(()).item()
+            U = tsr._new(_ops.scale(U.data, v), U.labels)
         out.append(lam_prev)
         out.append(lam_prev_inv[R, ] * U[L, ])
         if i == mps.nsites - 1:
