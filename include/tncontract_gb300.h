@@ -20,9 +20,10 @@
  *  - Functions return a TNC_* status; they never allocate device memory.
  *    Factorisations take a caller-provided workspace whose size is given by
  *    the matching *_workspace_size function.
- *  - Device-side failures (non-convergence, non-finite input, barrier
- *    timeout) are written to a device `info` word that the caller reads
- *    after synchronising; nothing traps or spins without bound.
+ *  - Device-side failures (non-convergence, non-finite input, a bounded
+ *    wait on a barrier, flag or step counter that gave up) are written to a
+ *    device `info` word that the caller reads after synchronising; nothing
+ *    traps or spins without bound.
  */
 #ifndef TNCONTRACT_GB300_H
 #define TNCONTRACT_GB300_H
