@@ -330,8 +330,8 @@ def run_ours(args):
     value = world * B * args.steps / elapsed
     # per-op durations: one more step of the same workload in which every
     # sweep brackets its QR, R-only QR and Jacobi calls by CUDA events on its
-    # instance's stream (timing events recorded on 8 concurrent streams slow
-    # the batch down, so the timed region above runs without them)
+    # instance's stream (timing events recorded on many concurrent streams
+    # slow the batch down, so the timed region above runs without them)
     profs = [(ctypes.c_double * 9)() for _ in range(B)]
     run_steps(1, profs)
     barrier()
