@@ -160,3 +160,42 @@ def test_high_rank_permute_and_trace_plans():
         got = np.trace(x.reshape(fs), axis1=b1, axis2=b2)
         ref = np.trace(x, axis1=a1, axis2=a2)
         assert np.allclose(got.reshape(ref.shape), ref)
+
+
+def test_sweep_flop_count():
+    """The metric's fixed flop count (per-site formula of the plain method's
+    bonds): a hand-computed small case, internal consistency, and the value
+    at the benchmark configuration."""
+    from tncontract_gb300 import workloads as W
+    f = W.sweep_flops(2, 2, 1, 1, complex_=False)
+    # apply 2*8; QR of 2x1: 2*2*1 - 2/3; R absorption 2*1*1*2; SVD of 2x1: 6*2 + 20; U S absorption 2*2*1*1
+    assert abs(f["total"] - (16 + (4 - 2.0 / 3.0) + 4 + 32 + 4)) < 1e-9
+    fc = W.sweep_flops(2, 2, 1, 1, complex_=True)
+    assert abs(fc["total"] - 4 * f["total"]) < 1e-9
+    big = W.sweep_flops(64, 2, 3, 256)
+    assert abs(sum(v for k, v in big.items() if k != "total") - big["total"]) < 1e-3 * big["total"]
+    assert abs(big["total"] / 1e12 - 1.5721156823466667) < 1e-9
+
+
+def test_balance_keeps_the_state():
+    import numpy as np
+    import tn_oracle as O
+    from tncontract_gb300 import engine as E
+    sites = O.random_mps(3, 8, 2, 6, np.complex128, normalise=True)
+    sites[2] = sites[2] * 1e-30
+    bal, log_norm = E.balance(sites)
+    assert all(abs(np.linalg.norm(a) - 1.0) < 1e-12 for a in bal)
+    n0 = O.mps_norm(sites)
+    n1 = O.mps_norm(bal) * np.exp(log_norm)
+    assert abs(n0 - n1) <= 1e-10 * n0
+    assert 1.0 - O.fidelity(sites, bal) < 1e-12
+
+
+def test_discarded_weight_rank():
+    from tncontract_gb300 import rank_model as RM
+    s = [1.0, 0.5, 0.1, 0.01]                      # s^2 total 1.2601
+    assert RM.dw_rank(s, 1e-3) == 3                # tail 1e-4 <= 1.26e-3
+    assert RM.dw_rank(s, 1e-3, chi=2) == 2
+    assert RM.dw_rank(s, 1e-2) == 2                # tail 0.0101 <= 0.012601
+    assert RM.dw_rank(s, 1.0) == 1                 # at least one value is kept
+    assert RM.dw_rank([0.0, 0.0], 1e-3) == 1
