@@ -199,3 +199,17 @@ def test_discarded_weight_rank():
     assert RM.dw_rank(s, 1e-2) == 2                # tail 0.0101 <= 0.012601
     assert RM.dw_rank(s, 1.0) == 1                 # at least one value is kept
     assert RM.dw_rank([0.0, 0.0], 1e-3) == 1
+
+
+def test_uneven_batch_specs():
+    """The uneven batch's instance list: 512 specs, ranges and dtypes of the
+    workload definition, deterministic in the seed."""
+    import numpy as np
+    from tncontract_gb300 import workloads as W
+    specs = W.config3_specs()
+    assert len(specs) == 512 and specs == W.config3_specs()
+    assert all(16 <= N <= 128 and d in (2, 3, 4) and 16 <= chi <= 256 for N, d, chi, _, _ in specs)
+    assert [dt for _, _, _, dt, _ in specs[:4]] == [np.float32, np.complex64, np.float32, np.complex64]
+    assert len({seed for *_, seed in specs}) == 512
+    assert {d for _, d, _, _, _ in specs} == {2, 3, 4}
+    assert W.config3_specs(seed=2) != specs
