@@ -11,7 +11,9 @@ random label sets (repeated labels included), ``consolidate_indices``,
 disconnected parts; same result or the same exception class); and random
 sequences of MPS operations (canonisations, compressions, reverse, gates,
 swaps, expectation values) compared by bond dimensions, labels, norm and
-fidelity.  Truncation to chi / threshold is applied to generic spectra only:
+fidelity; the Gamma-Lambda form (Schmidt values, canonical check, gates,
+expval, ptrace, converters); and PEPS inner products (exact and boundary
+MPS).  Truncation to chi / threshold is applied to generic spectra only:
 on an already canonical state the singular values are degenerate and the
 kept subspace is a gauge choice.
 """
@@ -161,6 +163,83 @@ def fuzz_mps(R, G, trials, rng):
     return bad
 
 
+def fuzz_canonical(R, G, trials, rng):
+    """Gamma-Lambda form: canonical_form_mps (Schmidt values, canonical-form
+    check, norm), a two-site gate on it, expval / ptrace, and the converters
+    back to left / right canonical form (same state)."""
+    import tn_oracle as O
+
+    def lam(net, host):
+        return [np.sort(np.abs(np.diag(host(net[2 * i]))))[::-1] for i in range(net.nsites_physical + 1)]
+
+    def sites(m, host):
+        out = []
+        for t in m:
+            lab = list(t.labels)
+            out.append(np.transpose(host(t), [lab.index(m.phys_label), lab.index(m.left_label),
+                                              lab.index(m.right_label)]))
+        return out
+
+    rh, gh = (lambda t: np.asarray(t.data)), (lambda t: t.to_numpy())
+    bad = 0
+    for trial in range(trials):
+        N, d, chi = rng.randint(2, 6), rng.randint(2, 3), rng.randint(1, 4)
+        dt = np.complex128 if rng.random() < 0.5 else np.float64
+        s = O.random_mps(1000 + trial, N, d, chi, dt, normalise=rng.random() < 0.5)
+        rc = R.onedim.onedim_core.canonical_form_mps(
+            R.onedim.MatrixProductState([R.Tensor(a, ["phys", "left", "right"]) for a in s]))
+        gc = G.onedim.canonical_form_mps(G.onedim.MatrixProductState([G.Tensor(a, ["phys", "left", "right"])
+                                                                      for a in s]))
+        if rc.bonddims() != gc.bonddims():
+            bad += 1
+            continue
+        bad += any(not np.allclose(a, b, rtol=1e-8, atol=1e-12) for a, b in zip(lam(rc, rh), lam(gc, gh)))
+        c1 = rc.check_canonical_form(threshold=1e-10, print_output=False)
+        c2 = gc.check_canonical_form(threshold=1e-10, print_output=False)
+        bad += [list(x) for x in c1] != [list(x) for x in c2]
+        i = rng.randint(0, N - 2)
+        gate = np.random.default_rng(trial).standard_normal((d, d, d, d))
+        e1 = complex(np.asarray(rc.expval(R.Tensor(gate, ["o1", "o2", "i1", "i2"]), i).data))
+        e2 = complex(gc.expval(G.Tensor(gate, ["o1", "o2", "i1", "i2"]), i).to_numpy())
+        bad += abs(e1 - e2) > 1e-8 * max(1.0, abs(e1))
+        p1, p2 = rc.ptrace(i), gc.ptrace(i)
+        bad += list(p1.labels) != list(p2.labels) or not np.allclose(np.asarray(p1.data), p2.to_numpy(), atol=1e-9)
+        rc.apply_gate(R.Tensor(gate, ["o1", "o2", "i1", "i2"]), i)
+        gc.apply_gate(G.Tensor(gate, ["o1", "o2", "i1", "i2"]), i)
+        for conv in ("canonical_to_left_canonical", "canonical_to_right_canonical"):
+            a = sites(getattr(R.onedim, conv)(rc.copy()), rh)
+            b = sites(getattr(G.onedim, conv)(gc.copy()), gh)
+            na, nb = O.mps_norm(a), O.mps_norm(b)
+            bad += abs(na - nb) > 1e-8 * max(na, 1e-300) or (na > 1e-12 and 1 - O.fidelity(a, b) > 1e-8)
+    return bad
+
+
+def fuzz_peps(R, G, trials, rng, nprng):
+    """inner_product_peps on random small lattices: exact and boundary-MPS
+    contraction at chi 2 and 4."""
+    def val(x):
+        if hasattr(x, "to_numpy"):
+            return complex(x.to_numpy().reshape(()))
+        if hasattr(x, "data"):
+            return complex(np.asarray(x.data).reshape(()))
+        return complex(x)
+
+    bad = 0
+    for trial in range(trials):
+        L, M, D, d = rng.randint(2, 4), rng.randint(2, 4), rng.randint(1, 2), 2
+        rows = [[nprng.random((d, 1 if r == 0 else D, 1 if c == M - 1 else D, 1 if r == L - 1 else D,
+                               1 if c == 0 else D)) for c in range(M)] for r in range(L)]
+        legs = ["phys", "up", "right", "down", "left"]
+        rp = R.twodim.SquareLatticePEPS([[R.Tensor(a, legs) for a in r] for r in rows])
+        gp = G.twodim.SquareLatticePEPS([[G.Tensor(a, legs) for a in r] for r in rows])
+        for kw in ({"exact_contract": True}, {"exact_contract": False, "chi": 4},
+                   {"exact_contract": False, "chi": 2}):
+            o1 = outcome(lambda: R.twodim.inner_product_peps(rp, rp, **kw))
+            o2 = outcome(lambda: G.twodim.inner_product_peps(gp, gp, **kw))
+            bad += o1[0] != o2[0] or (o1[0] == "ok" and abs(val(o1[1]) - val(o2[1])) > 1e-8 * abs(val(o1[1])))
+    return bad
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     trials = int(sys.argv[2]) if len(sys.argv) > 2 else 200
@@ -171,7 +250,9 @@ def main():
     rng, nprng = random.Random(0), np.random.default_rng(0)
     with cpu_ops():
         res = {"tensor": fuzz_tensor(R, G, trials, rng, nprng), "con": fuzz_con(R, G, trials, rng, nprng),
-               "mps": fuzz_mps(R, G, max(trials // 2, 1), rng)}
+               "mps": fuzz_mps(R, G, max(trials // 2, 1), rng),
+               "canonical": fuzz_canonical(R, G, max(trials // 3, 1), rng),
+               "peps": fuzz_peps(R, G, max(trials // 10, 1), rng, nprng)}
     print("mismatches:", res)
     return 1 if any(res.values()) else 0
 
