@@ -213,3 +213,20 @@ def test_uneven_batch_specs():
     assert len({seed for *_, seed in specs}) == 512
     assert {d for _, d, _, _, _ in specs} == {2, 3, 4}
     assert W.config3_specs(seed=2) != specs
+
+
+def test_trace_of_unequal_axes_host():
+    """contract_internal over axes of different lengths sums the common
+    leading diagonal, as np.trace does (the reference's behaviour)."""
+    import numpy as np
+    import tncontract_gb300 as tn
+    rng = np.random.default_rng(6)
+    with cpu_ops():
+        for shape, a1, a2 in [((2, 3), 0, 1), ((4, 2, 3), 0, 2), ((3, 2, 5, 2), 2, 0), ((1, 3), 1, 0)]:
+            x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+            labels = ["l%d" % i for i in range(len(shape))]
+            t = tn.Tensor(x, list(labels))
+            t.contract_internal(labels[a1], labels[a2])
+            ref = np.trace(x, axis1=a1, axis2=a2)
+            assert t.labels == [l for i, l in enumerate(labels) if i not in (a1, a2)]
+            assert np.allclose(t.to_numpy(), ref)

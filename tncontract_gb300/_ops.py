@@ -304,6 +304,22 @@ def slice_last(data, k):
     return out
 
 
+def slice_axis(data, axis, k):
+    """Contiguous copy of ``data`` with axis ``axis`` cut to its first k
+    entries (``data`` itself when k is the full extent): one 2-D block copy
+    of the (before, axis x after) view."""
+    data = data.contiguous()
+    n = data.shape[axis]
+    if k == n:
+        return data
+    after = int(np.prod(data.shape[axis + 1:], dtype=np.int64))
+    rows = int(np.prod(data.shape[:axis], dtype=np.int64))
+    out = empty(tuple(data.shape[:axis]) + (k,) + tuple(data.shape[axis + 1:]), data.dtype)
+    if out.numel():
+        copy2d(data, rows, k * after, n * after, out, k * after)
+    return out
+
+
 def diag_matrix(s, dtype):
     n = s.shape[0]
     out = empty((n, n), dtype)

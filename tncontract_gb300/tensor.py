@@ -301,13 +301,16 @@ class Tensor():
         self.labels = new_labels
 
     def contract_internal(self, label1, label2, index1=0, index2=0):
-        """``tensor.py:318-334``: trace over two labelled axes."""
+        """``tensor.py:318-334``: trace over two labelled axes.  Axes of
+        different lengths are traced over their common leading diagonal, as
+        ``np.trace`` does (the longer axis is cut first)."""
         i1 = [i for i, x in enumerate(self.labels) if x == label1][index1]
         i2 = [i for i, x in enumerate(self.labels) if x == label2][index2]
-        if self.data.shape[i1] != self.data.shape[i2]:
-            raise ValueError("diag requires an array of at least two dimensions "
-                             "with equal axis lengths")
-        self.data = _ops.trace(self.data, i1, i2)
+        data = self.data
+        n1, n2 = data.shape[i1], data.shape[i2]
+        if n1 != n2:
+            data = _ops.slice_axis(data, i1 if n1 > n2 else i2, min(n1, n2))
+        self.data = _ops.trace(data, i1, i2)
         self.labels = [l for j, l in enumerate(self.labels) if j not in (i1, i2)]
 
     trace = contract_internal
