@@ -12,8 +12,9 @@ disconnected parts; same result or the same exception class); and random
 sequences of MPS operations (canonisations, compressions, reverse, gates,
 swaps, expectation values) compared by bond dimensions, labels, norm and
 fidelity; the Gamma-Lambda form (Schmidt values, canonical check, gates,
-expval, ptrace, converters); and PEPS inner products (exact and boundary
-MPS).  Truncation to chi / threshold is applied to generic spectra only:
+expval, ptrace, converters); the chain helpers (frob_distance_squared,
+contract_virtual_indices, ladder_contract, the multi-index contraction); and
+PEPS inner products (exact and boundary MPS).  Truncation to chi / threshold is applied to generic spectra only:
 on an already canonical state the singular values are degenerate and the
 kept subspace is a gauge choice.
 """
@@ -214,6 +215,46 @@ def fuzz_canonical(R, G, trials, rng):
     return bad
 
 
+def fuzz_chain_helpers(R, G, trials, rng, nprng):
+    """frob_distance_squared, contract_virtual_indices (open and periodic:
+    the periodic trace can pair legs of different lengths, which np.trace
+    accepts), ladder_contract over every start / end / option, and
+    contract_multi_index_tensor_with_one_dim_array."""
+    import tn_oracle as O
+    bad = 0
+    for trial in range(trials):
+        N, chi = rng.randint(2, 5), rng.randint(1, 3)
+        s1 = O.random_mps(2000 + trial, N, 2, chi, np.complex128)
+        s2 = O.random_mps(3000 + trial, N, 2, chi + 1, np.complex128)
+        mk = lambda M, s: M.onedim.MatrixProductState([M.Tensor(a, ["phys", "left", "right"]) for a in s])
+        r1, r2, g1, g2 = mk(R, s1), mk(R, s2), mk(G, s1), mk(G, s2)
+        v1, v2 = complex(R.onedim.frob_distance_squared(r1, r2)), complex(G.onedim.frob_distance_squared(g1, g2))
+        bad += abs(v1 - v2) > 1e-8 * max(1.0, abs(v1))
+        st = rng.randint(0, N - 1)
+        en, per = rng.randint(st + 1, N), rng.choice([True, False])
+        o1 = outcome(lambda: R.onedim.contract_virtual_indices(r1, st, en, periodic_boundaries=per))
+        o2 = outcome(lambda: G.onedim.contract_virtual_indices(g1, st, en, periodic_boundaries=per))
+        bad += o1[0] != o2[0] or (o1[0] == "ok" and not same_tensor(o1[1], o2[1]))
+        st = rng.randint(0, N - 1)
+        kw = dict(start=st, end=rng.randint(st, N - 1), complex_conjugate_array1=rng.choice([True, False]),
+                  return_intermediate_contractions=rng.choice([True, False]))
+        o1 = outcome(lambda: R.onedim.ladder_contract(r1, r2, "phys", "phys", **kw))
+        o2 = outcome(lambda: G.onedim.ladder_contract(g1, g2, "phys", "phys", **kw))
+        if o1[0] != o2[0]:
+            bad += 1
+        elif o1[0] == "ok":
+            a = o1[1] if kw["return_intermediate_contractions"] else [o1[1]]
+            b = o2[1] if kw["return_intermediate_contractions"] else [o2[1]]
+            bad += len(a) != len(b) or any(not same_tensor(x, y) for x, y in zip(a, b))
+        T = nprng.standard_normal([2] * N)
+        o1 = outcome(lambda: R.onedim.contract_multi_index_tensor_with_one_dim_array(
+            R.Tensor(T, ["p"] * N), r1, "p", "phys"))
+        o2 = outcome(lambda: G.onedim.contract_multi_index_tensor_with_one_dim_array(
+            G.Tensor(T, ["p"] * N), g1, "p", "phys"))
+        bad += o1[0] != o2[0] or (o1[0] == "ok" and not same_tensor(o1[1], o2[1]))
+    return bad
+
+
 def fuzz_peps(R, G, trials, rng, nprng):
     """inner_product_peps on random small lattices: exact and boundary-MPS
     contraction at chi 2 and 4."""
@@ -252,6 +293,7 @@ def main():
         res = {"tensor": fuzz_tensor(R, G, trials, rng, nprng), "con": fuzz_con(R, G, trials, rng, nprng),
                "mps": fuzz_mps(R, G, max(trials // 2, 1), rng),
                "canonical": fuzz_canonical(R, G, max(trials // 3, 1), rng),
+               "chain_helpers": fuzz_chain_helpers(R, G, max(trials // 2, 1), rng, nprng),
                "peps": fuzz_peps(R, G, max(trials // 10, 1), rng, nprng)}
     print("mismatches:", res)
     return 1 if any(res.values()) else 0
