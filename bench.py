@@ -43,8 +43,8 @@ STAGGER = 0.02
 METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, complex128)"
 # dram bytes (read + write) per call of the dominant native op at the
 # workload's bulk shape (the Jacobi kernel of tnc_svd_rows on the 512 x 512
-# complex64 triangular factor: 2.412 MB read + 0.470 MB written), from the
-# ncu summary profiles/jacobi_block_c64_512x512.md; absent = not captured.
+# complex64 triangular factor: 2.412 MB read + 0.470 MB written), from an
+# ncu capture of that kernel at that shape; absent = not captured.
 TRAFFIC_PER_CALL = {"tnc_svd_rows": 2.882e6}
 
 
