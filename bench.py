@@ -56,11 +56,11 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nsites", type=int, default=N_SITES)
     p.add_argument("--chi", type=int, default=CHI)
-    p.add_argument("--cpu-sample-sites", type=int, default=28)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batch", type=int, default=12, help="independent instances per GPU")
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 drop-in comparison")
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 engine arm")
+    p.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the plain FP64 engine arm")
     p.add_argument("--workload", default="tfim", choices=["tfim", "uneven"],
                    help="tfim: the headline sweep; uneven: the uneven batch of independent MPS")
     p.add_argument("--instances", type=int, default=512, help="instances of the uneven batch")
@@ -197,41 +197,41 @@ class ClockSampler:
 # ------------------------------------------------------------------ CPU legs
 
 
-def cpu_sample(nsites, chi, steps=1, target=N_SITES):
-    """Reference algorithm (oracle restatement, NumPy/LAPACK) on N=nsites at
-    the full bond dimension; returns (seconds per sample, the flop ratio of
-    the sample to a sweep of ``target`` sites)."""
+def oracle_sweep(seed, nsites, chi, discarded_fraction=None):
+    """One full apply + svd_compress sweep of instance ``seed`` through the
+    reference algorithm on the host cores (the NumPy restatement in oracle/,
+    the reference's own LAPACK / BLAS calls, every host thread OpenBLAS
+    takes).  Returns (output sites, seconds of the sweep)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import tn_oracle as O
     from tncontract_gb300 import workloads as W
-    sites = O.random_mps(0, nsites, PHYS, chi, np.complex128, normalise=True)
-    mpo = O.tfim_mpo(nsites)
-    times = []
-    for _ in range(steps):
-        t = time.perf_counter()
-        O.apply_compress_sweep(sites, mpo, chi)
-        times.append(time.perf_counter() - t)
-    ratio = W.sweep_flops(nsites, PHYS, MPO_D, chi)["total"] / W.sweep_flops(target, PHYS, MPO_D, chi)["total"]
-    return times, ratio
+    sites = W.random_mps_arrays(seed, nsites, PHYS, chi, np.complex128, normalise=True)
+    mpo = W.tfim_mpo_arrays(nsites)
+    t = time.perf_counter()
+    out = O.apply_compress_sweep(sites, mpo, chi, discarded_fraction=discarded_fraction)
+    return out, time.perf_counter() - t
 
 
 def run_reference(args):
+    """The reference algorithm on the machine's host cores: every step is one
+    full sweep of the benchmark workload (N sites at chi, complex128), no
+    sampling or scaling.  One untimed warm-up sweep (the CPU path has no
+    caches to fill beyond the BLAS threads)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     cores = os.cpu_count()
-    cpu_sample(8, 16)  # warm the BLAS threads
-    w = max(args.warmup, 0)
-    if w:
-        cpu_sample(args.cpu_sample_sites, args.chi, steps=1, target=args.nsites)
-    times, ratio = cpu_sample(args.cpu_sample_sites, args.chi, steps=max(args.steps, 1), target=args.nsites)
-    per_sweep = statistics.median(times) / ratio
-    value = 1.0 / per_sweep
-    sample = ("apply+svd_compress on N=%d sites at chi=%d (same d, D, dtype), scaled by the "
-              "algorithmic flop ratio %.4f to N=%d" % (args.cpu_sample_sites, args.chi, ratio, args.nsites))
+    oracle_sweep(0, 8, 16)  # start the BLAS threads
+    if args.warmup > 0:
+        oracle_sweep(0, args.nsites, args.chi)
+    times = [oracle_sweep(0, args.nsites, args.chi)[1] for _ in range(max(args.steps, 1))]
+    total = sum(times)
+    value = len(times) / total
+    sample = ("%d full sweeps (apply + svd_compress, N=%d, chi=%d, complex128), one at a time, after one "
+              "warm-up sweep" % (len(times), args.nsites, args.chi))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / len(times) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic (seeded random MPS, TFIM MPO)",
             "config": {"workload": "tfim_apply_svd_compress", "nsites": args.nsites, "phys_dim": PHYS,
@@ -243,10 +243,30 @@ def run_reference(args):
     return 0
 
 
+def errors_vs_oracle(got_sites, log_norm, discarded, ref_sites, ref_discarded):
+    """Per-output error of one instance against the FP64 oracle's result of
+    the same sweep: fidelity error of the compressed states, the largest
+    per-bond difference of the discarded fraction of the squared spectrum,
+    and the relative error of the state norm."""
+    import numpy as np
+    import tn_oracle as O
+    got = [np.asarray(a, dtype=np.complex128) for a in got_sites]
+    f = O.fidelity(ref_sites, got)
+    n_ref = O.mps_norm(ref_sites)
+    n_got = O.mps_norm(got)
+    if log_norm is not None:   # sites without the norm folded in
+        n_got = float(np.exp(log_norm))
+    dw = max(abs(a - b) for a, b in zip(discarded, ref_discarded)) if discarded else None
+    return {"fidelity_error": 1.0 - f, "discarded_weight_max_abs_error": dw,
+            "discarded_weight_max": max(ref_discarded) if ref_discarded else None,
+            "norm_rel_error": abs(n_got - n_ref) / n_ref, "norm": n_got, "norm_oracle": n_ref}
+
+
 # ------------------------------------------------------------------ GPU leg
 
 
 def run_ours(args):
+    import ctypes
     import numpy as np
     import torch
     import torch.distributed as dist
@@ -260,53 +280,46 @@ def run_ours(args):
 
     import __graft_entry__
     __graft_entry__.build()
-    import tncontract_gb300 as tn
-    from tncontract_gb300 import _lib, _ops
+    from tncontract_gb300 import _lib
     from tncontract_gb300 import engine as E
     from tncontract_gb300 import workloads as W
 
     N, chi, B = args.nsites, args.chi, args.batch
     warm = max(args.warmup, 3)
-    # instance b of rank r uses seed (r * B + b); every instance is a full workload
+    core = "fp64" if args.precision == "mixed" else None
+    # instance b of rank r uses seed (r * B + b); every instance is a full
+    # workload; the caller's data is complex128 on the host
     host_batch = [W.random_mps_arrays(rank * B + b, N, PHYS, chi, np.complex128, normalise=True)
                   for b in range(B)]
     host_mpo = W.tfim_mpo_arrays(N)
-    dt = E.compute_dtype(args.precision, True)
-    np_dt = np.complex64 if dt == torch.complex64 else np.complex128
-    # FP32 storage needs balanced sites (see engine.balance); the log norms
-    # travel with the host buffers
-    balanced = [E.balance(sites) for sites in host_batch]
-    log_norms = [ln for _, ln in balanced]
-    pinned_batch = [[torch.from_numpy(a.astype(np_dt)).pin_memory() for a in sites] for sites, _ in balanced]
-    pinned_mpo = [torch.from_numpy(w.astype(np_dt)).pin_memory() for w in host_mpo]
-    # e2e bytes per step: every sweep job copies its instance's sites and the MPO
-    h2d = sum(a.numel() * a.element_size() for sites in pinned_batch for a in sites) + \
-        B * sum(w.numel() * w.element_size() for w in pinned_mpo)
-
-    dev_batch = [E.to_sites(sites, dt) for sites in pinned_batch]
-    dev_mpo = E.to_sites(pinned_mpo, dt)
     streams = [torch.cuda.Stream() for _ in range(B)]
-
-    # the timed work: K steps of B sweeps as one queue of K*B jobs on B
-    # streams (continuous batching: an instance that finishes its sweep takes
-    # the next one), each sweep one native call (tnc_sweep_apply_compress)
-    import ctypes
-    last = [None] * B
-    OPS = ("tnc_qr", "tnc_qr_r", "tnc_svd_rows")
-
-    def sweep_job(b, prof=None):
-        def job():
-            last[b] = E.apply_compress_native(dev_batch[b], dev_mpo, chi, log_norm_in=log_norms[b], profile=prof)
-        return job
-
-    def run_steps(k, profs=None):
-        jobs = [sweep_job(b, profs[j * B + b] if profs else None) for j in range(k) for b in range(B)]
-        E.run_queue(jobs, B, streams=streams, stagger=STAGGER)
 
     def barrier():
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
+
+    # ---- value: inputs resident in HBM (balanced and cast before timing)
+    dt = E.compute_dtype(args.precision, True)
+    balanced = [E.balance(sites) for sites in host_batch]
+    log_norms = [ln for _, ln in balanced]
+    dev_batch = [E.to_sites(sites, dt) for sites, _ in balanced]
+    dev_mpo = E.to_sites(host_mpo, dt)
+    last = [None] * B
+    last_stats = [None] * B
+    OPS = ("tnc_qr", "tnc_qr_r", "tnc_svd_rows", "tnc_svd_rows_fp64_finish")
+
+    def sweep_job(b, prof=None, precision_core=core, batch=dev_batch, mpo=dev_mpo, out=last, stats=last_stats):
+        def job():
+            st = E.SweepStats()
+            out[b] = E.apply_compress_native(batch[b], mpo, chi, log_norm_in=log_norms[b], profile=prof,
+                                             stats=st, core=precision_core)
+            stats[b] = st
+        return job
+
+    def run_steps(k, profs=None, **kw):
+        jobs = [sweep_job(b, profs[j * B + b] if profs else None, **kw) for j in range(k) for b in range(B)]
+        E.run_queue(jobs, B, streams=streams, stagger=STAGGER)
 
     run_steps(warm)
     barrier()
@@ -320,7 +333,6 @@ def run_ours(args):
         run_steps(args.steps)
         ev1.record(st)
         barrier()
-    out = last
     launches = _lib.kernel_launches() - launches0
     elapsed = ev0.elapsed_time(ev1) / 1e3
     if world > 1:
@@ -328,27 +340,34 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
     value = world * B * args.steps / elapsed
-    # per-op durations: one more step of the same workload in which every
-    # sweep brackets its QR, R-only QR and Jacobi calls by CUDA events on its
+    out_sites = [[a.cpu().numpy() for a in o] for o in last]
+    out_stats = list(last_stats)
+
+    # per-op durations: one more step in which every sweep brackets its QR,
+    # R-only QR, Jacobi and FP64 finish calls by CUDA events on its
     # instance's stream (timing events recorded on many concurrent streams
     # slow the batch down, so the timed region above runs without them)
-    profs = [(ctypes.c_double * 9)() for _ in range(B)]
+    profs = [(ctypes.c_double * 12)() for _ in range(B)]
     run_steps(1, profs)
     barrier()
     timed = {op: (sum(p[3 * o + 1] for p in profs), sum(p[3 * o] for p in profs), sum(p[3 * o + 2] for p in profs))
              for o, op in enumerate(OPS)}
+    timed = {k: v for k, v in timed.items() if v[0] > 0}
     dom_name = max(timed.items(), key=lambda kv: kv[1][1])[0]
 
-    # end to end through the public API: pinned host arrays in, host arrays
-    # out, every sweep job copying its own inputs and results
+    # ---- e2e: through the public host-array API (engine.apply_compress_host):
+    # the caller's pinned complex128 arrays in, complex128 host arrays out;
+    # the host->device copy, balancing and casting on the device, the sweep,
+    # the cast back and the device->host copy are inside the timed region
+    pinned_batch = [[torch.from_numpy(a).pin_memory() for a in sites] for sites in host_batch]
+    pinned_mpo = [torch.from_numpy(w).pin_memory() for w in host_mpo]
+    h2d = sum(a.numel() * a.element_size() for sites in pinned_batch for a in sites) + \
+        B * sum(w.numel() * w.element_size() for w in pinned_mpo)
     e2e_last = [None] * B
 
     def e2e_job(b):
         def job():
-            sites = E.to_sites(pinned_batch[b], dt)
-            mpo = E.to_sites(pinned_mpo, dt)
-            r = E.apply_compress_native(sites, mpo, chi, log_norm_in=log_norms[b])
-            e2e_last[b] = [t.cpu().numpy() for t in r]
+            e2e_last[b] = E.apply_compress_host(pinned_batch[b], pinned_mpo, chi, precision=args.precision)
         return job
 
     E.run_queue([e2e_job(b) for b in range(B)], B, streams=streams, stagger=STAGGER)
@@ -357,42 +376,45 @@ def run_ours(args):
     E.run_queue([e2e_job(b) for _ in range(args.steps) for b in range(B)], B, streams=streams, stagger=STAGGER)
     barrier()
     e2e_el = time.perf_counter() - t0
-    res = e2e_last
     if world > 1:
         t = torch.tensor([e2e_el], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_el = float(t.item())
-    d2h = sum(a.nbytes for r in res for a in r)  # per step: B instances' results
+    d2h = sum(a.nbytes for r in e2e_last for a in r)  # per step: B instances' results
     e2e_value = world * B * args.steps / e2e_el
 
-    # plain FP64 drop-in path (this project's straightforward FP64 method) on
-    # instance 0, and the fidelity error of the measured path against it
+    # ---- the plain FP64 method of this project: the same native sweep and
+    # work queue in complex128 end to end (QR, Jacobi, products, decision)
     extra = {}
-    if rank == 0 and not args.no_plain:
-        psi = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in host_batch[0]])
-        mpo = tn.onedim.MatrixProductOperator([tn.Tensor(w, ["physout", "physin", "left", "right"])
-                                               for w in host_mpo])
-
-        def plain():
-            phi = tn.onedim.contract_mps_mpo(psi, mpo)
-            phi.svd_compress(chi=chi)
-            return phi
-
-        plain()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ref = plain()
-        torch.cuda.synchronize()
-        t_plain = time.perf_counter() - t0
-        ref_sites = []
-        for t in ref:
-            lab = t.labels
-            ref_sites.append(_ops.permute(t.data, [lab.index(ref.phys_label), lab.index(ref.left_label),
-                                                   lab.index(ref.right_label)]))
-        fid = E.fidelity(ref_sites, [_ops.cast(x, torch.complex128) for x in out[0]])
-        extra = {"plain_fp64_sweeps_per_s": 1.0 / t_plain,
-                 "speedup_vs_plain_fp64": value / (1.0 / t_plain),
-                 "fidelity_error_vs_plain_fp64": 1.0 - fid}
+    fp64_sites, fp64_stats = None, None
+    if not args.no_plain:
+        dt64 = torch.complex128
+        batch64 = [E.to_sites(sites, dt64) for sites, _ in balanced]
+        mpo64 = E.to_sites(host_mpo, dt64)
+        last64, stats64 = [None] * B, [None] * B
+        kw = dict(precision_core=None, batch=batch64, mpo=mpo64, out=last64, stats=stats64)
+        run_steps(1, **kw)   # warm-up (workspaces, first launches)
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(st)
+        run_steps(args.fp64_steps, **kw)
+        e1.record(st)
+        barrier()
+        t64 = e0.elapsed_time(e1) / 1e3
+        if world > 1:
+            t = torch.tensor([t64], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t64 = float(t.item())
+        v64 = world * B * args.fp64_steps / t64
+        fp64_sites = [a.cpu().numpy() for a in last64[0]]
+        fp64_stats = stats64[0]
+        extra["plain_fp64"] = {"value": v64, "unit": "sweeps/s", "steps": args.fp64_steps, "warmup": 1,
+                               "path": "the same native sweep and %d-stream work queue in complex128 (FP64 QR, "
+                                       "Jacobi, products and truncation decision)" % B}
+        extra["speedup_vs_plain_fp64"] = value / v64
+        del batch64, mpo64, last64
 
     name = dom_name
     ncalls, ms, flops = timed[name]
@@ -403,26 +425,31 @@ def run_ours(args):
     except Exception:
         peak, peak_src = 1900.0, "fallback"
     achieved = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
-    fp_note = ("FP32 CUDA-core arithmetic (Jacobi rotations, Householder); frac is against the "
-               "measured bf16 tensor peak, frac_of_fp32_nominal against GB300's nominal FP32 rate "
-               "(152 SMs x 128 FMA x 2 x 2.07 GHz = 80.5 TFLOP/s)")
+    fp64_op = name.endswith("fp64_finish")
+    pipe = ("FP64", 1.25) if fp64_op else ("FP32", 80.5)
+    fp_note = ("CUDA-core arithmetic (Jacobi rotations, Householder); frac is against the measured bf16 tensor "
+               "peak, frac_of_pipe_nominal against GB300's nominal %s CUDA-core rate (%s TFLOP/s%s); flops are "
+               "%s" % (pipe[0], pipe[1], "" if fp64_op else ": 152 SMs x 128 FMA x 2 x 2.07 GHz",
+                       "the FP64 Jacobi's executed flops (14 n^2 L per rotating sweep, 4 n^2 L for the checking "
+                       "one)" if fp64_op else "the op's fixed algorithmic count"))
     roofline = {"bound": "tensor", "kernel": name, "launches": ncalls, "achieved": achieved,
                 "measured": "CUDA events around every %s call, recorded by the native sweep on its instance's "
                             "stream in one profiled step of the same workload after the timed region (%d streams "
                             "run concurrently, so durations include time shared with other instances)" % (name, B),
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": peak_src,
-                "traffic": TRAFFIC_PER_CALL.get(name), "fp32_nominal_tflops": 80.5,
-                "frac_of_fp32_nominal": achieved / 80.5, "note": fp_note}
+                "traffic": TRAFFIC_PER_CALL.get(name), "pipe": pipe[0], "pipe_nominal_tflops": pipe[1],
+                "frac_of_pipe_nominal": achieved / pipe[1], "note": fp_note}
     tot_ms = sum(x[1] for x in timed.values())
-    # of the three factorisation stages' event time in the timed region
     share = {k: round(v[1] / tot_ms, 4) for k, v in timed.items() if tot_ms > 0}
-
+    dtype_name = {"mixed": "c64+f64core", "fp32": "c64", "fp64": "c128"}[args.precision]
+    path = {"mixed": "engine (mixed: complex64 sites and FP32 products and QR, FP32 Jacobi finished by an FP64 "
+                     "Jacobi on every bond core, truncation decided on FP64 singular values)",
+            "fp32": "engine (fp32)", "fp64": "engine (fp64)"}[args.precision]
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": warm, "ms_per_step": elapsed / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64" if dt == torch.complex64 else "c128",
-            "data": "synthetic (seeded random MPS, TFIM MPO)",
-            "config": {"workload": "tfim_apply_svd_compress", "path": "engine (%s)" % args.precision,
+            "dtype": dtype_name, "data": "synthetic (seeded random MPS, TFIM MPO)",
+            "config": {"workload": "tfim_apply_svd_compress", "path": path, "precision": args.precision,
                        "batch_per_gpu": B, "nsites": N, "phys_dim": PHYS, "mpo_bond": MPO_D, "chi": chi,
                        "input_dtype": "complex128", "parallelism": "replicas" if world > 1 else "single",
                        "scheduling": "K steps x %d sweeps as one work queue on %d CUDA streams (continuous "
@@ -431,7 +458,9 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (%d MPS of 67 MB complex64 on the device, 0.6 GB applied "
                              "each)" % B},
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d // 1,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h,
+                    "path": "engine.apply_compress_host: pinned complex128 host arrays -> device, balance and "
+                            "cast on the device, native sweep, complex128 host arrays back"},
             "gpu_launches": launches,
             "roofline": roofline,
             "stage_share": share,
@@ -439,12 +468,25 @@ def run_ours(args):
             "sweep_tflop": W.sweep_flops(N, PHYS, MPO_D, chi)["total"] / 1e12}
     line.update(extra)
     if rank == 0 and not args.no_cpu_baseline:
-        times, ratio = cpu_sample(args.cpu_sample_sites, chi, steps=1, target=N)
-        v = ratio / times[0]
-        line["cpu_baseline"] = {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": "apply+svd_compress on N=%d sites at chi=%d, scaled by the "
-                                          "algorithmic flop ratio %.4f to N=%d" % (
-                                              args.cpu_sample_sites, chi, ratio, N)}
+        # the FP64 oracle on instance 0 (seed 0): timed as the CPU baseline,
+        # and the reference result every output of the GPU paths is checked
+        # against
+        ref_df = []
+        ref, t_cpu = oracle_sweep(0, N, chi, discarded_fraction=ref_df)
+        line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": "one full sweep (N=%d, chi=%d, complex128) of instance 0" % (N, chi)}
+        st0 = out_stats[0]
+        errs = {args.precision: errors_vs_oracle(out_sites[0], None if st0.norm_folded else st0.log_norm,
+                                                 st0.discarded, ref, ref_df)}
+        errs[args.precision]["bond_dims_match"] = [1] + list(st0.bonds) + [1] == \
+            [1] + [a.shape[2] for a in ref[:-1]] + [1]
+        if fp64_sites is not None:
+            errs["fp64"] = errors_vs_oracle(fp64_sites, None if fp64_stats.norm_folded else fp64_stats.log_norm,
+                                            fp64_stats.discarded, ref, ref_df)
+            errs["fp64"]["bond_dims_match"] = list(fp64_stats.bonds) == [a.shape[2] for a in ref[:-1]]
+        e2e0 = e2e_last[0]
+        errs["e2e_" + args.precision] = {"fidelity_error": 1.0 - __import__("tn_oracle").fidelity(ref, e2e0)}
+        line["errors_vs_fp64_oracle"] = errs
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -259,24 +259,39 @@ int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
  * mps_bonds[n_sites+1], mpo_bonds[n_sites+1] (both ends 1); out_bonds
  * [n_sites+1] and out_offsets[n_sites] (byte offset in `work` of each
  * compressed site, (phys, out_bonds[i], out_bonds[i+1])) are written.
+ * core: TNC_CORE_STORAGE (0) factors every bond core in the storage
+ * precision; TNC_CORE_FP64 (1, F32 / C64 storage only) finishes the Jacobi of
+ * each core (rows up to 512 for C64, 1024 for F32) in FP64 after the
+ * storage-precision Jacobi, and takes the singular values, the truncation
+ * decision and U from the FP64 rows.  core_tol: that FP64 Jacobi's
+ * tolerance (<= 0: 1e-8, pairs of rows orthogonal to 1e-8 relative; U is
+ * stored back in single precision and the singular values' error is second
+ * order in it).  The core changes the workspace size.
+ * out_discarded (HOST, may be NULL): n_sites-1 doubles, [i] = the fraction of
+ * the squared singular values discarded at the bond between sites i and i+1.
  * *log_norm: in, the natural log of the input state's norm factor; out, that
  * of the output.  *folded = 1 when that factor (except its s_max part) was
  * representable and folded into the first site.  block_rows as for
- * tnc_svd_rows (0 = 8).  profile (HOST, may be NULL): 9 doubles, for op o
- * (0 the QR of the left sweep, 1 the R-only QR of M^H, 2 the Jacobi)
- * profile[3o] += milliseconds (CUDA events on `stream`), [3o+1] += calls,
- * [3o+2] += the op's fixed algorithmic flops.  Returns TNC_ERR_ARG for a
- * zero state. */
+ * tnc_svd_rows (0 = 8).  profile (HOST, may be NULL): 12 doubles, for op o
+ * (0 the QR of the left sweep, 1 the R-only QR of M^H, 2 the Jacobi, 3 its
+ * FP64 finish) profile[3o] += milliseconds (CUDA events on `stream`),
+ * [3o+1] += calls, [3o+2] += the op's fixed algorithmic flops (for op 3 the
+ * flops the FP64 Jacobi executed: 14 n^2 L per rotating sweep and 4 n^2 L for
+ * the last, checking one, n rows of length L, complex; a third of that
+ * real).  Returns TNC_ERR_ARG for a zero state. */
+enum { TNC_CORE_STORAGE = 0, TNC_CORE_FP64 = 1 };
 int tnc_sweep_workspace_size(int dtype, int n_sites, int64_t d,
                              const int64_t *mps_bonds, const int64_t *mpo_bonds,
-                             size_t *bytes);
+                             int core, size_t *bytes);
 int tnc_sweep_apply_compress(int dtype, int n_sites, int64_t d,
                              const void *const *sites, const int64_t *mps_bonds,
                              const void *const *mpo, const int64_t *mpo_bonds,
                              int64_t chi, double threshold, int block_rows,
-                             void *work, size_t work_bytes, int64_t *out_bonds,
-                             int64_t *out_offsets, double *log_norm,
-                             int *folded, double *profile, void *stream);
+                             int core, double core_tol, void *work,
+                             size_t work_bytes, int64_t *out_bonds,
+                             int64_t *out_offsets, double *out_discarded,
+                             double *log_norm, int *folded, double *profile,
+                             void *stream);
 
 /* ------------------------------------------------------------ learned rank
  * Kernels of the rank predictor (a small MLP trained on singular spectra the

@@ -205,15 +205,17 @@ def left_canonise_qr(sites, normalise=False):
 
 
 def left_canonise_svd(sites, chi=None, threshold=1e-14, normalise=False,
-                      spectra=None, discarded=None):
+                      spectra=None, discarded=None, discarded_fraction=None):
     """SVD branch of ``left_canonise``, ``onedim_core.py:296-358``.
 
     Each site's singular values are divided by the largest one, whose product
     is tracked in ``norm`` (``:332-334``); ``s/s_max > threshold`` then
     ``[:chi]`` are kept (``:336-339``); ``S V`` is absorbed into the next site
     (``:347-351``); the last site is normalised or multiplied by ``norm``
-    (``:301-314``).  If given, ``spectra`` / ``discarded`` receive per bond the
-    kept singular values (un-normalised) and the discarded weight sum(s^2).
+    (``:301-314``).  If given, ``spectra`` / ``discarded`` /
+    ``discarded_fraction`` receive per bond the kept singular values
+    (un-normalised), the discarded weight sum(s[k:]^2) and that weight as a
+    fraction of sum(s^2).
     """
     sites = [a.copy() for a in sites]
     N = len(sites)
@@ -242,6 +244,8 @@ def left_canonise_svd(sites, chi=None, threshold=1e-14, normalise=False,
             spectra.append(s[:k].copy())
         if discarded is not None:
             discarded.append(float(np.sum(s[k:] ** 2)))
+        if discarded_fraction is not None:
+            discarded_fraction.append(float(np.sum(s[k:] ** 2) / np.sum(s ** 2)))
         sites[i] = u[:, :k].reshape(d, l, k)
         sv = sn[:k, None] * vh[:k]
         nxt = np.tensordot(sv, sites[i + 1], (1, 1))  # (k, phys, right)
@@ -250,11 +254,11 @@ def left_canonise_svd(sites, chi=None, threshold=1e-14, normalise=False,
 
 
 def right_canonise_svd(sites, chi=None, threshold=1e-14, normalise=False,
-                       spectra=None, discarded=None):
+                       spectra=None, discarded=None, discarded_fraction=None):
     """``right_canonise`` = reverse, left-canonise, reverse
     (``onedim_core.py:360-378``).  Spectra are reported right-to-left."""
     return mps_reverse(left_canonise_svd(mps_reverse(sites), chi, threshold,
-                                         normalise, spectra, discarded))
+                                         normalise, spectra, discarded, discarded_fraction))
 
 
 def left_canonical_form_mps(sites, chi=0, threshold=1e-14, normalise=False):
@@ -263,13 +267,15 @@ def left_canonical_form_mps(sites, chi=0, threshold=1e-14, normalise=False):
 
 
 def svd_compress_method(sites, chi=None, threshold=1e-15, normalise=False,
-                        spectra=None, discarded=None):
+                        spectra=None, discarded=None, discarded_fraction=None):
     """``MatrixProductState.svd_compress``, ``onedim_core.py:463-484``: QR left
-    sweep, divide by the norm, truncating SVD right sweep, restore the norm."""
+    sweep, divide by the norm, truncating SVD right sweep, restore the norm.
+    Per-bond outputs of the truncating sweep (see ``left_canonise_svd``) are
+    reported right-to-left."""
     s1 = left_canonise_qr(sites, normalise=False)
     nrm = np.linalg.norm(s1[-1])
     s1[-1] = s1[-1] / nrm
-    s2 = right_canonise_svd(s1, chi, threshold, False, spectra, discarded)
+    s2 = right_canonise_svd(s1, chi, threshold, False, spectra, discarded, discarded_fraction)
     if not normalise:
         s2[0] = s2[0] * nrm
     return s2
@@ -432,6 +438,25 @@ def random_mps(seed, N, d, chi, dtype=np.float64, normalise=False):
     return sites
 
 
+def graded_mps(seed, N, d, chi, decades=20.0, dtype=np.float64):
+    """Seeded MPS whose bond spectra fall over ``decades`` orders of
+    magnitude: Gaussian sites whose right-bond columns are scaled by
+    10**(-decades * j / (r - 1)).  A relative truncation threshold (not the
+    bond cap) then decides every rank, as it does for the boundary MPS of a
+    PEPS norm network.  Not in the reference (an input generator)."""
+    rng = np.random.default_rng(seed)
+    bonds = [1] + [min(chi, d ** (i + 1), d ** (N - 1 - i)) for i in range(N - 1)] + [1]
+    out = []
+    for i in range(N):
+        r = bonds[i + 1]
+        a = rng.standard_normal((d, bonds[i], r))
+        if np.iscomplexobj(np.zeros(0, dtype)):
+            a = a + 1j * rng.standard_normal((d, bonds[i], r))
+        lam = 10.0 ** (-decades * np.arange(r) / max(r - 1, 1))
+        out.append((a * lam[None, None, :]).astype(dtype))
+    return out
+
+
 def tfim_mpo(N, J=1.0, h=0.5, dtype=np.float64):
     """Transverse-field Ising MPO, H = -J sum Z_i Z_{i+1} - h sum X_i, bond D=3,
     lower-triangular W = [[I,0,0],[Z,0,0],[-hX,-JZ,I]] with boundary row/column
@@ -500,8 +525,13 @@ def random_peps(seed, nrows, ncols, D, d, dtype=np.float64):
     return rows
 
 
-def apply_compress_sweep(sites, mpo, chi, threshold=1e-15):
+def apply_compress_sweep(sites, mpo, chi, threshold=1e-15, discarded_fraction=None):
     """One unit of the benchmark: ``contract_mps_mpo`` then
     ``MatrixProductState.svd_compress(chi)`` (QR left sweep, truncating SVD
-    right sweep)."""
-    return svd_compress_method(contract_mps_mpo(sites, mpo), chi, threshold)
+    right sweep).  ``discarded_fraction`` (a list) receives the discarded
+    fraction of the squared spectrum per bond, bonds left to right."""
+    df = [] if discarded_fraction is not None else None
+    out = svd_compress_method(contract_mps_mpo(sites, mpo), chi, threshold, discarded_fraction=df)
+    if df is not None:
+        discarded_fraction.extend(df[::-1])
+    return out

@@ -229,6 +229,25 @@ def gen_config2(tn, store, meta, N, chi, tag):
         pack_list(tag + "_f_spectra", spectra_of(to_sites(f, tn)), store)
 
 
+def gen_graded(tn, store, meta):
+    """svd_compress(threshold=1e-14) without a bond cap on MPS whose spectra
+    fall over 20 decades (oracle.graded_mps): the threshold decides every
+    rank, so the bond dimensions pin the rank rule itself.  Real float64 and
+    complex128 inputs; the seeds are chosen so that every singular value the
+    truncations see lies at least 0.4 decades from the threshold (a count
+    closer to it would depend on rounding)."""
+    for tag, dt, seed in (("gr", np.float64, 11), ("grc", np.complex128, 2)):
+        sites = O.graded_mps(seed, 16, 2, 32, 20.0, dt)
+        mps = tn.onedim.MatrixProductState([tn.Tensor(a, ["phys", "left", "right"]) for a in sites])
+        m = mps.copy()
+        m.svd_compress(threshold=1e-14)
+        meta[tag + "_seed"] = seed
+        meta[tag + "_bonds"] = [int(x) for x in m.bonddims()]
+        meta[tag + "_input_bonds"] = [1] + [a.shape[2] for a in sites]
+        store[tag + "_norm"] = np.array(m.norm())
+        pack_list(tag + "_spectra", spectra_of(to_sites(m, tn)), store)
+
+
 def gen_peps(tn, store, meta, L, D, d, chi, tag, seed=2):
     rows = O.random_peps(seed, L, L, D, d)
     peps = tn.twodim.SquareLatticePEPS(
@@ -528,7 +547,9 @@ def gen_con_cases(tn, store, meta):
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
-    ref_path = args[0] if args else "/root/reference"
+    if not args:
+        raise SystemExit("usage: python tests/golden/gen_golden.py /path/to/tncontract-checkout [--only=NAME ...]")
+    ref_path = args[0]
     tn = _ref(ref_path)
     if not only or "labels_and_fixture" in only:
         store, meta = {}, {}
@@ -540,12 +561,14 @@ def main():
     for fn, job in [("config1", lambda s, m: gen_config1(tn, s, m)),
                     ("config2_small", lambda s, m: gen_config2(tn, s, m, 12, 16, "c2s")),
                     ("config2_chi128", lambda s, m: gen_config2(tn, s, m, 64, 128, "c2")),
+                    ("config2_chi256", lambda s, m: gen_config2(tn, s, m, 64, 256, "c2x")),
                     ("peps", lambda s, m: (gen_peps(tn, s, m, 4, 2, 2, 4, "p4"),
                                            gen_peps(tn, s, m, 8, 4, 2, 16, "p8c16"),
                                            gen_peps(tn, s, m, 8, 4, 2, 64, "p8c64"))),
                     ("onedim_extras", lambda s, m: gen_onedim_extras(tn, s, m)),
                     ("con_cases", lambda s, m: gen_con_cases(tn, s, m)),
-                    ("onedim_edges", lambda s, m: gen_onedim_edges(tn, s, m))]:
+                    ("onedim_edges", lambda s, m: gen_onedim_edges(tn, s, m)),
+                    ("graded", lambda s, m: gen_graded(tn, s, m))]:
         if only and fn not in only:
             continue
         s, m = {}, {}

@@ -1,6 +1,6 @@
 """``bench.py --impl reference`` (the reference algorithm timed on the host
-cores) prints one JSON line with the contract's keys, on CPU, at a small
-size."""
+cores, every step one full sweep) prints one JSON line with the contract's
+keys, on CPU, at a small size."""
 import json
 import os
 import subprocess
@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_json_line():
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-           "--warmup", "0", "--nsites", "8", "--chi", "8", "--cpu-sample-sites", "6"]
+           "--warmup", "0", "--nsites", "8", "--chi", "8"]
     out = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
@@ -23,4 +23,5 @@ def test_reference_arm_json_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["config"]["nsites"] == 8 and d["config"]["chi"] == 8
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert "full sweep" in d["cpu_baseline"]["sample"] and "scaled" not in d["cpu_baseline"]["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

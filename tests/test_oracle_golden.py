@@ -84,6 +84,43 @@ def test_config2_chi128_apply_compress():
     assert abs(O.mps_norm(c) - float(np.real(g["c2_norm_m"]))) < 1e-10
 
 
+def test_config2_chi256_apply_compress():
+    """The benchmark's own configuration (N=64, chi=256, complex128): the
+    oracle against the reference's bond dimensions, norm, fidelity to the
+    applied state and per-bond spectra.  About half a minute of LAPACK."""
+    g, m = K.load("config2_chi256")
+    N, chi = 64, 256
+    sites = O.random_mps(0, N, 2, chi, np.complex128, normalise=True)
+    phi = O.contract_mps_mpo(sites, O.tfim_mpo(N))
+    df = []
+    c = O.svd_compress_method(phi, chi, discarded_fraction=df)
+    assert [1] + [a.shape[2] for a in c] == m["c2x_m_bonds"]
+    assert abs(O.mps_norm(c) - float(np.real(g["c2x_norm_m"]))) < 1e-10
+    assert abs(O.fidelity(phi, c) - float(np.real(g["c2x_fid_m_phi"]))) < 1e-10
+    for s, s_ref in zip(O.bond_spectra(c), K.unpack(g, "c2x_m_spectra")):
+        assert K.close(s, s_ref, 1e-10)
+    # each truncation keeps (1 - df) of the current squared norm, so their
+    # product is the reference's squared norm ratio of the result to phi
+    assert len(df) == N - 1 and all(0.0 <= x < 1.0 for x in df)
+    kept = float(np.prod([1.0 - x for x in df]))
+    ratio = (float(np.real(g["c2x_norm_m"])) / float(np.real(g["c2x_norm_phi"]))) ** 2
+    assert abs(kept - ratio) < 1e-10 * ratio
+
+
+def test_graded_rank_rule():
+    """Spectra over 20 decades, svd_compress(threshold=1e-14) without a cap:
+    the threshold decides every rank (tests/golden/graded)."""
+    g, m = K.load("graded")
+    for tag, dt in (("gr", np.float64), ("grc", np.complex128)):
+        sites = O.graded_mps(m[tag + "_seed"], 16, 2, 32, 20.0, dt)
+        assert [1] + [a.shape[2] for a in sites] == m[tag + "_input_bonds"]
+        c = O.svd_compress_method(sites, None, 1e-14)
+        assert [1] + [a.shape[2] for a in c] == m[tag + "_bonds"]
+        assert abs(O.mps_norm(c) - float(np.real(g[tag + "_norm"]))) < 1e-12 * float(np.real(g[tag + "_norm"]))
+        for s, s_ref in zip(O.bond_spectra(c), K.unpack(g, tag + "_spectra")):
+            assert K.close(s, s_ref, 1e-10)
+
+
 def test_peps_small_against_reference():
     g, m = K.load("peps")
     layer = O.double_layer(O.random_peps(2, 4, 4, 2, 2))

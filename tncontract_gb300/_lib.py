@@ -16,6 +16,7 @@ from . import _build
 F32, F64, C64, C128 = 0, 1, 2, 3
 OK, ERR_ARG, ERR_NOT_CONVERGED, ERR_NONFINITE, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_TOO_LARGE = range(8)
 OP_N, OP_T, OP_C, OP_R = 0, 1, 2, 3
+CORE_STORAGE, CORE_FP64 = 0, 1
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -48,9 +49,10 @@ SIGNATURES = {
     "tnc_qr_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_qr": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, C.c_size_t, _vp, _vp],
     "tnc_qr_r_workspace_size": [_int, _i64, _i64, _int, _psz],
-    "tnc_sweep_workspace_size": [_int, _int, _i64, _pi64, _pi64, _psz],
+    "tnc_sweep_workspace_size": [_int, _int, _i64, _pi64, _pi64, _int, _psz],
     "tnc_sweep_apply_compress": [_int, _int, _i64, C.POINTER(_vp), _pi64, C.POINTER(_vp), _pi64, _i64, C.c_double,
-                                 _int, _vp, C.c_size_t, _pi64, _pi64, _pdbl, _pint, _pdbl, _vp],
+                                 _int, _int, C.c_double, _vp, C.c_size_t, _pi64, _pi64, _pdbl, _pdbl, _pint, _pdbl,
+                                 _vp],
     "tnc_qr_r": [_int, _i64, _i64, _vp, _int, _vp, _vp, C.c_size_t, _vp, _vp],
     "tnc_svd_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_svd": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, C.c_size_t, _vp, _vp],

@@ -22,6 +22,15 @@
 //                                  at the rounding-noise floor 4 eps |M|_F;
 //                                  U = normalised rows;  S V^H = U^H M;
 //                                  P_i = U;  P_{i-1} <- P_{i-1} (S V^H)^T / s_max.
+// With the FP64 core (core = 1, single-precision storage only) the Jacobi of
+// every truncating bond runs twice: the storage-precision Jacobi above brings
+// the rows of R to orthogonality at the FP32 rounding level, then the rows are
+// widened to FP64 and a one-sided FP64 Jacobi finishes them (from a start that
+// close, one rotating sweep and one checking sweep at the default tolerance
+// kCoreTol);
+// the singular values, the truncation decision (s / s_max > threshold, at most
+// chi) and U come from the FP64 rows.  The products around the core stay in
+// the storage precision.
 // All buffers are carved from one caller workspace sized for the un-truncated
 // bond dimensions (tnc_sweep_workspace_size); nothing is allocated.
 #include "tnc_common.cuh"
@@ -49,7 +58,20 @@ struct Dims {
   std::vector<int64_t> bp;  // applied bonds b_i * D_i
   int64_t max_site = 0, max_r = 0, max_u = 0, max_sv = 0, max_kmin = 0;
   size_t fact = 0;          // largest factorisation / GEMM workspace
+  bool core64 = false;      // FP64 Jacobi finish of the bond cores
 };
+
+// Default tolerance of the FP64 finish: |<w_i, w_j>| <= tol |w_i| |w_j| for every
+// pair of rows.  U is stored back in single precision, so orthogonality below
+// the FP32 rounding level is not kept, and the singular values' error is second
+// order in the tolerance (1e-16 relative at 1e-8): from the FP32-converged
+// start (pairs at ~1e-5) one rotating sweep and one checking sweep suffice.
+constexpr double kCoreTol = 1e-8;
+
+// the FP64 type that finishes the Jacobi of a single-precision core
+inline int core_dtype(int dt) { return dt == TNC_C64 ? TNC_C128 : TNC_F64; }
+// rows of the register-resident FP64 Jacobi (complex128 rows hold 512 entries)
+inline int64_t core_rows_limit(int dt) { return dt == TNC_C64 ? 512 : 1024; }
 
 bool fp32_class(int dt) { return dt == TNC_F32 || dt == TNC_C64; }
 
@@ -60,15 +82,23 @@ size_t tc_ws(int dt, int64_t m, int64_t n, int64_t k, int64_t batch) {
   return b;
 }
 
+// The sweep's absorption products run on the CUDA-core GEMM (round-to-nearest
+// FMA).  The tensor cores' FP32 accumulation truncates toward zero, which
+// biases every product's magnitude down by ~1e-8 x K: over the 190 products
+// of a sweep at chi = 256 that shrank the state's norm by 1.6e-3 (its
+// direction, and so the fidelity, was unaffected).
 bool use_tc(int dt, int64_t m, int64_t n, int64_t k, int64_t batch) {
-  return fp32_class(dt) && (m < n ? m : n) >= 64 && k >= 32 && (double)m * n * k * batch >= (double)(1 << 21) &&
-         batch <= 65535;
+  (void)dt, (void)m, (void)n, (void)k, (void)batch;
+  return false;
 }
 
 int64_t rows_limit(int dt) { return fp32_class(dt) ? 1024 : 512; }
 
 // upper bounds of every buffer over the whole sweep
-int plan(int dt, int n_sites, int64_t d, const int64_t* b, const int64_t* D, Dims& P) {
+int plan(int dt, int n_sites, int64_t d, const int64_t* b, const int64_t* D, int core, Dims& P) {
+  if (core != 0 && core != 1) return TNC_ERR_ARG;
+  if (core == 1 && !fp32_class(dt)) return TNC_ERR_ARG;  // the FP64 core finishes single-precision cores
+  P.core64 = core == 1;
   P.bp.resize(n_sites + 1);
   for (int i = 0; i <= n_sites; ++i) {
     if (b[i] <= 0 || D[i] <= 0) return TNC_ERR_ARG;
@@ -98,6 +128,10 @@ int plan(int dt, int n_sites, int64_t d, const int64_t* b, const int64_t* D, Dim
     const int64_t mr = m < rows_limit(dt) ? m : rows_limit(dt), kr = mr < n ? mr : n;
     if (tnc_svd_rows_workspace_size(dt, kr, mr, &x) != TNC_OK) return TNC_ERR_ARG;
     f = x > f ? x : f;
+    if (P.core64) {
+      if (tnc_svd_rows_workspace_size(core_dtype(dt), kr, mr, &x) != TNC_OK) return TNC_ERR_ARG;
+      f = x > f ? x : f;
+    }
     if (m > rows_limit(dt)) {
       if (tnc_svd_workspace_size(dt, kmin, m, &x) != TNC_OK) return TNC_ERR_ARG;
       f = x > f ? x : f;
@@ -121,6 +155,9 @@ int plan(int dt, int n_sites, int64_t d, const int64_t* b, const int64_t* D, Dim
 struct Buffers {
   std::vector<void*> slot;
   void *scratch, *rbuf, *wbuf, *ubuf, *svbuf, *S, *fact;
+  void *w64a = nullptr, *w64b = nullptr;  // FP64 core: widened rows, finished rows
+  double* S64 = nullptr;
+  int64_t* order64 = nullptr;
   int64_t* order;
   int64_t* kdev;
   double* dnorm;
@@ -140,6 +177,13 @@ size_t carve(Carve& c, int n_sites, int64_t d, const Dims& P, size_t es, size_t 
   B.kdev = (int64_t*)c.take(sizeof(int64_t));
   B.dnorm = (double*)c.take(sizeof(double));
   B.info = (int*)c.take(4 * sizeof(int));
+  if (P.core64) {
+    const size_t es64 = 2 * es;  // complex64 -> complex128, float -> double
+    B.w64a = c.take((size_t)P.max_r * es64);
+    B.w64b = c.take((size_t)P.max_r * es64);
+    B.S64 = (double*)c.take((size_t)P.max_kmin * sizeof(double));
+    B.order64 = (int64_t*)c.take((size_t)P.max_kmin * sizeof(int64_t));
+  }
   B.fact = c.take(P.fact);
   return c.off;
 }
@@ -178,10 +222,11 @@ int device_status(const int* info, cudaStream_t st) {
 // Optional per-op timing of a sweep on the caller's stream: for op o,
 // prof[3o] += milliseconds, prof[3o+1] += calls, prof[3o+2] += the op's fixed
 // algorithmic flops (QR 2mn^2 - 2n^3/3, SVD 6mn^2 + 20n^3, complex x4).
-// Ops: 0 the QR of the left sweep, 1 the R-only QR of M^H, 2 the Jacobi.
+// Ops: 0 the QR of the left sweep, 1 the R-only QR of M^H, 2 the Jacobi,
+// 3 the FP64 finish of the Jacobi (FP64 core only).
 struct Prof {
   double* out = nullptr;
-  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev[8] = {};
   bool ok = false;
   explicit Prof(double* o) : out(o) {
     if (!out) return;
@@ -240,14 +285,14 @@ int64_t rank_rule(const std::vector<R>& s, int64_t chi, double threshold, double
 
 template <typename T>
 int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const int64_t* b, const void* const* mpo,
-               const int64_t* D, int64_t chi, double threshold, int block_rows, void* work, size_t wb,
-               int64_t* out_bonds, int64_t* out_offsets, double* log_norm, int* folded, double* profile,
-               cudaStream_t st) {
+               const int64_t* D, int64_t chi, double threshold, int block_rows, int core, double core_tol, void* work,
+               size_t wb, int64_t* out_bonds, int64_t* out_offsets, double* out_discarded, double* log_norm,
+               int* folded, double* profile, cudaStream_t st) {
   typedef typename traits<T>::real R;
   const bool cplx = traits<T>::is_complex;
   Prof prof(profile);
   Dims P;
-  if (int rc = plan(dt, n_sites, d, b, D, P)) return rc;
+  if (int rc = plan(dt, n_sites, d, b, D, core, P)) return rc;
   Carve c{(char*)work, 0};
   Buffers B;
   const size_t need = carve(c, n_sites, d, P, sizeof(T), sizeof(R), B);
@@ -298,6 +343,7 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
   // 3. truncating SVD right sweep
   double norm_acc = 1.0;
   std::vector<R> s_host((size_t)P.max_kmin);
+  std::vector<double> sd;  // the spectrum the truncation decision reads
   for (int i = n_sites - 1; i >= 1; --i) {
     const int64_t l = sl[i], r = sr[i], m = d * r, n = l, kmin = m < n ? m : n;
     {  // M = P_i as (d, r, l)
@@ -326,17 +372,60 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
         return rc;
     }
     prof.end(2, st);
-    if (cudaMemcpyAsync(s_host.data(), B.S, (size_t)kmin * sizeof(R), cudaMemcpyDeviceToHost, st) != cudaSuccess)
-      return TNC_ERR_CUDA;
-    if (int stq = device_status(B.info, st)) return stq;
-    prof.add(2, svd_flops(kmin, m, cplx));
-    s_host.resize((size_t)kmin);
-    const int64_t k = rank_rule<R>(s_host, chi, threshold, eps);
-    s_host.resize((size_t)P.max_kmin);
-    const double smax = (double)s_host[0];
+    // the FP64 finish of the core (rows up to the FP64 register limit)
+    const bool core_path = P.core64 && rows_path && m <= core_rows_limit(dt);
+    if (core_path) {
+      if (int stq = device_status(B.info, st)) return stq;
+      prof.add(2, svd_flops(kmin, m, cplx));
+      const int cdt = core_dtype(dt);
+      if (int rc = tnc_cast(dt, cdt, kmin * m, B.wbuf, B.w64a, st)) return rc;
+      if (tnc_svd_rows_workspace_size(cdt, kmin, m, &xb) != TNC_OK || xb > factb) return TNC_ERR_WORKSPACE;
+      prof.begin(3, st);
+      if (int rc = tnc_svd_rows(cdt, kmin, m, B.w64a, B.w64b, B.S64, B.order64, 0,
+                                core_tol > 0 ? core_tol : kCoreTol, block_rows, B.fact, factb, B.info, st))
+        return rc;
+      prof.end(3, st);
+      sd.resize((size_t)kmin);
+      if (cudaMemcpyAsync(sd.data(), B.S64, (size_t)kmin * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess)
+        return TNC_ERR_CUDA;
+      int hinfo[2] = {0, 0};
+      if (cudaMemcpyAsync(hinfo, B.info, sizeof(hinfo), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return TNC_ERR_CUDA;
+      if (cudaStreamSynchronize(st) != cudaSuccess) return TNC_ERR_CUDA;
+      if (hinfo[0]) return hinfo[0];
+      {  // executed FP64 flops: rotating sweeps, then the checking one
+        const double nn = (double)kmin * kmin * m, sweeps = hinfo[1] > 0 ? hinfo[1] : 1;
+        prof.add(3, ((sweeps - 1.0) * 14.0 + 4.0) * nn / (cplx ? 1.0 : 3.0));
+      }
+    } else {
+      if (cudaMemcpyAsync(s_host.data(), B.S, (size_t)kmin * sizeof(R), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return TNC_ERR_CUDA;
+      if (int stq = device_status(B.info, st)) return stq;
+      prof.add(2, svd_flops(kmin, m, cplx));
+      sd.assign(s_host.begin(), s_host.begin() + kmin);
+    }
+    // the truncation decision (FP64 values with the FP64 core), capped at the
+    // storage type's rounding-noise floor
+    const int64_t k = rank_rule<double>(sd, chi, threshold, eps);
+    const double smax = sd.empty() ? 0.0 : sd[0];
     if (!(smax > 0.0) || k < 1) return TNC_ERR_ARG;  // zero state
+    if (out_discarded) {
+      double tot = 0.0, dis = 0.0;
+      for (int64_t j = 0; j < kmin; ++j) {
+        tot += sd[j] * sd[j];
+        if (j >= k) dis += sd[j] * sd[j];
+      }
+      out_discarded[i - 1] = tot > 0 ? dis / tot : 0.0;
+    }
     // U (m x k)
-    if (rows_path) {
+    if (core_path) {
+      const int cdt = core_dtype(dt);
+      if (cudaMemcpyAsync(B.kdev, &k, sizeof(int64_t), cudaMemcpyHostToDevice, st) != cudaSuccess) return TNC_ERR_CUDA;
+      if (int rc = tnc_gather_rows(cdt, B.w64b, m, B.order64, B.kdev, k, B.S64, 1, B.w64a, st)) return rc;
+      if (int rc = tnc_cast(cdt, dt, m * k, B.w64a, B.ubuf, st)) return rc;
+      if (cudaStreamSynchronize(st) != cudaSuccess) return TNC_ERR_CUDA;  // k lives on this frame
+    } else if (rows_path) {
       if (cudaMemcpyAsync(B.kdev, &k, sizeof(int64_t), cudaMemcpyHostToDevice, st) != cudaSuccess) return TNC_ERR_CUDA;
       if (int rc = tnc_gather_rows(dt, B.wbuf, m, B.order, B.kdev, k, B.S, 1, B.ubuf, st)) return rc;
       if (cudaStreamSynchronize(st) != cudaSuccess) return TNC_ERR_CUDA;  // k lives on this frame
@@ -389,10 +478,10 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
 using namespace tnc;
 
 extern "C" int tnc_sweep_workspace_size(int dtype, int n_sites, int64_t d, const int64_t* mps_bonds,
-                                        const int64_t* mpo_bonds, size_t* bytes) {
+                                        const int64_t* mpo_bonds, int core, size_t* bytes) {
   if (!elem_size(dtype) || n_sites < 2 || d <= 0 || !mps_bonds || !mpo_bonds || !bytes) return TNC_ERR_ARG;
   Dims P;
-  if (int rc = plan(dtype, n_sites, d, mps_bonds, mpo_bonds, P)) return rc;
+  if (int rc = plan(dtype, n_sites, d, mps_bonds, mpo_bonds, core, P)) return rc;
   Carve c{nullptr, 0};
   Buffers B;
   const size_t rs = (dtype == TNC_F32 || dtype == TNC_C64) ? 4 : 8;
@@ -402,15 +491,17 @@ extern "C" int tnc_sweep_workspace_size(int dtype, int n_sites, int64_t d, const
 
 extern "C" int tnc_sweep_apply_compress(int dtype, int n_sites, int64_t d, const void* const* sites,
                                         const int64_t* mps_bonds, const void* const* mpo, const int64_t* mpo_bonds,
-                                        int64_t chi, double threshold, int block_rows, void* work, size_t work_bytes,
-                                        int64_t* out_bonds, int64_t* out_offsets, double* log_norm, int* folded,
-                                        double* profile, void* stream) {
+                                        int64_t chi, double threshold, int block_rows, int core, double core_tol,
+                                        void* work, size_t work_bytes, int64_t* out_bonds, int64_t* out_offsets,
+                                        double* out_discarded, double* log_norm, int* folded, double* profile,
+                                        void* stream) {
   if (n_sites < 2 || d <= 0 || !sites || !mps_bonds || !mpo || !mpo_bonds || !work || !out_bonds || !out_offsets ||
       !log_norm || !folded || chi < 0)
     return TNC_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   TNC_DISPATCH(dtype, T,
                return sweep_impl<T>(dtype, n_sites, d, sites, mps_bonds, mpo, mpo_bonds, chi, threshold, block_rows,
-                                    work, work_bytes, out_bonds, out_offsets, log_norm, folded, profile, st));
+                                    core, core_tol, work, work_bytes, out_bonds, out_offsets, out_discarded, log_norm,
+                                    folded, profile, st));
   return TNC_ERR_ARG;
 }

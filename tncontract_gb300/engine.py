@@ -35,10 +35,17 @@ import torch
 from . import _lib as L
 from . import _ops
 
-_DT = {"fp32": (torch.complex64, torch.float32), "fp64": (torch.complex128, torch.float64)}
+_DT = {"fp32": (torch.complex64, torch.float32), "fp64": (torch.complex128, torch.float64),
+       "mixed": (torch.complex64, torch.float32)}
+# precision -> how the native sweep factors each bond core
+CORE = {"fp32": L.CORE_STORAGE, "fp64": L.CORE_STORAGE, "mixed": L.CORE_FP64}
 
 
 def compute_dtype(precision, is_complex):
+    """Storage dtype of a precision: "fp64" complex128 / float64; "fp32" and
+    "mixed" complex64 / float32 ("mixed" finishes every bond core's Jacobi
+    in FP64 and decides the truncation on the FP64 singular values, see
+    ``apply_compress_native``)."""
     return _DT[precision][0 if is_complex else 1]
 
 
@@ -341,16 +348,22 @@ def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0
 
 
 def apply_compress_native(sites, mpo, chi, threshold=1e-15, log_norm_in=0.0, stats=None, block_rows=0,
-                          profile=None):
+                          profile=None, core=None, core_tol=0.0):
     """``apply_compress`` as one native call (``tnc_sweep_apply_compress``):
     the same algorithm, rank rule and norm handling, with the whole sweep run
     by the library so the calling thread stays out of the interpreter (and
     off its lock) until the sweep ends.  Sites and MPO as for
     ``apply_compress``; returns the compressed sites (compact copies; the
     sweep's workspace is released), ``stats.log_norm`` / ``stats.bonds`` /
-    ``stats.norm_folded`` when ``stats`` is given.  ``profile``: a ctypes
-    array of 9 doubles accumulating per-op CUDA-event time, calls and
-    algorithmic flops (QR, R-only QR, Jacobi), or None."""
+    ``stats.norm_folded`` / ``stats.discarded`` (per bond, the discarded
+    fraction of the squared singular values, bonds left to right) when
+    ``stats`` is given.  ``profile``: a ctypes array of 12 doubles
+    accumulating per-op CUDA-event time, calls and algorithmic flops (QR,
+    R-only QR, Jacobi, its FP64 finish), or None.  ``core``: "fp64" finishes
+    the Jacobi of every bond core in FP64 and takes the spectrum, the
+    truncation decision and U from it (single-precision sites only; the
+    "mixed" precision), None / "storage" factors in the storage precision;
+    ``core_tol``: the FP64 Jacobi's tolerance (0: its default)."""
     import ctypes as C
     N = len(sites)
     dt = sites[0].dtype
@@ -362,19 +375,21 @@ def apply_compress_native(sites, mpo, chi, threshold=1e-15, log_norm_in=0.0, sta
     b_arr = (C.c_int64 * (N + 1))(*bonds)
     m_arr = (C.c_int64 * (N + 1))(*mbonds)
     code = _ops.code(dt)
+    core_code = {None: L.CORE_STORAGE, "storage": L.CORE_STORAGE, "fp64": L.CORE_FP64}[core]
     sz = C.c_size_t()
     L.check("tnc_sweep_workspace_size",
-            L.lib().tnc_sweep_workspace_size(code, N, d, b_arr, m_arr, C.byref(sz)))
+            L.lib().tnc_sweep_workspace_size(code, N, d, b_arr, m_arr, core_code, C.byref(sz)))
     ws = torch.empty(int(sz.value), dtype=torch.uint8, device=sites[0].device)
     s_arr = (C.c_void_p * N)(*[s.data_ptr() for s in sites])
     w_arr = (C.c_void_p * N)(*[w.data_ptr() for w in mpo])
     out_b = (C.c_int64 * (N + 1))()
     out_o = (C.c_int64 * N)()
+    out_d = (C.c_double * (N - 1))()
     lnorm = C.c_double(float(log_norm_in))
     folded = C.c_int(0)
     st = L.lib().tnc_sweep_apply_compress(code, N, d, s_arr, b_arr, w_arr, m_arr, int(chi or 0), float(threshold),
-                                          int(block_rows), C.c_void_p(ws.data_ptr()), sz.value, out_b, out_o,
-                                          C.byref(lnorm), C.byref(folded), profile,
+                                          int(block_rows), core_code, float(core_tol), C.c_void_p(ws.data_ptr()),
+                                          sz.value, out_b, out_o, out_d, C.byref(lnorm), C.byref(folded), profile,
                                           C.c_void_p(torch.cuda.current_stream().cuda_stream))
     if st == L.ERR_ARG:
         raise ValueError("zero state in the sweep (or bad arguments)")
@@ -391,10 +406,49 @@ def apply_compress_native(sites, mpo, chi, threshold=1e-15, log_norm_in=0.0, sta
         out.append(view.clone())
     if stats is not None:
         stats.bonds = list(out_b)[1:N]
+        stats.discarded = list(out_d)
         stats.log_norm = lnorm.value
         stats.norm_folded = bool(folded.value)
         stats.norm = float(np.exp(lnorm.value)) if abs(lnorm.value) < 700 else float("inf")
     return out
+
+
+def apply_compress_host(sites, mpo, chi, precision="mixed", threshold=1e-15, stats=None):
+    """The sweep for a caller that holds the state in host memory, as
+    tncontract's users do: ``sites`` (phys, left, right) and ``mpo``
+    (physout, physin, left, right) are host arrays (NumPy or CPU torch
+    tensors; pinned tensors copy asynchronously) of any float / complex
+    dtype.  On the current stream the inputs are copied to the device,
+    balanced (``balance``) and cast to the storage dtype of ``precision``,
+    the sweep runs as one native call (``apply_compress_native``; "mixed"
+    finishes every bond core in FP64), and the result comes back as host
+    arrays of the input's precision class (complex128 / float64 for double
+    input) with the state's norm in the first site, as
+    ``MatrixProductState.svd_compress`` leaves it (onedim_core.py:463-484)."""
+    def dev(a):
+        t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
+        return t.to(device=_ops.device(), non_blocking=True)
+    d_sites = [dev(a) for a in sites]
+    d_mpo = [dev(w) for w in mpo]
+    cplx = any(t.is_complex() for t in d_sites + d_mpo)
+    dt = compute_dtype(precision, cplx)
+    out_dt = torch.complex128 if cplx else torch.float64
+    bal, log_norm = balance(d_sites)
+    st = stats if stats is not None else SweepStats()
+    out = apply_compress_native([_ops.cast(a, dt) for a in bal], [_ops.cast(w, dt) for w in d_mpo], chi,
+                                threshold=threshold, log_norm_in=log_norm, stats=st,
+                                core="fp64" if precision == "mixed" else None)
+    res = [_ops.cast(o, out_dt) for o in out]
+    if not st.norm_folded and abs(st.log_norm) < 700:
+        # the factor did not fit the storage type; it fits the output's
+        res[0] = _ops.scale(res[0], float(np.exp(st.log_norm - _log_norm_of(res))))
+    return [r.cpu().numpy() for r in res]
+
+
+def _log_norm_of(sites):
+    """log of the norm of the state held by ``sites`` (device)."""
+    v = inner_product(sites, sites).real
+    return 0.5 * float(np.log(v)) if v > 0 else 0.0
 
 
 def compress(sites, chi, threshold=1e-15, stats=None, log_norm_in=0.0, fold_norm=True):
