@@ -499,89 +499,135 @@ def run_uneven(args):
     [16, 128], d in {2, 3, 4}, chi in [16, 256], float32 / complex64
     alternating, ``workloads.config3_specs``), each left-canonised, svd-
     compressed to chi // 2 (QR sweep + truncating SVD sweep, one native call
-    with an identity MPO) and its norm evaluated.  Inputs are generated on
-    the device from per-instance seeds (Gaussian entries, each site scaled to
-    unit expected norm) before the timed region; the jobs run heaviest first
-    on a work queue of ``--batch`` streams.  A sample of instances is checked
-    against the oracle (fidelity error) and timed on the host cores as the
-    CPU baseline, scaled to the whole batch by the flop ratio."""
+    with an identity MPO) and its norm evaluated.  Under torchrun every rank
+    runs its flop-balanced share (``workloads.run_sharded``: the same split
+    on every rank, no data exchanged), the time is the max over ranks, and
+    the per-instance scalars (log norm, bonds) are gathered to rank 0.
+    Inputs are generated on the device from per-instance seeds (Gaussian
+    entries, each site scaled to unit expected norm) before the timed region;
+    the jobs run heaviest first on a work queue of ``--batch`` streams.  A
+    sample of instances is checked against the oracle on the rank that ran
+    it (fidelity error) and timed on rank 0's host cores as the CPU baseline,
+    scaled to the whole batch by the flop ratio."""
     import numpy as np
     import torch
+    import torch.distributed as dist
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     import __graft_entry__
     __graft_entry__.build()
     from tncontract_gb300 import _ops
     from tncontract_gb300 import engine as E
     from tncontract_gb300 import workloads as W
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     specs = W.config3_specs(1, args.instances)
+    mine = set(W.partition_by_flops(specs, world)[rank])
     tdt = {np.float32: torch.float32, np.complex64: torch.complex64}
-    inputs, idents = [], {}
-    for (N, d, chi, dt, seed) in specs:
+    inputs, idents = {}, {}
+    for i in sorted(mine):
+        N, d, chi, dt, seed = specs[i]
         td = tdt[dt]
         bonds = [1] + [chi] * (N - 1) + [1]
         sites = []
-        for i in range(N):
-            a = _ops.fill_gaussian((d, bonds[i], bonds[i + 1]), td, seed * 1000 + i)
+        for j in range(N):
+            a = _ops.fill_gaussian((d, bonds[j], bonds[j + 1]), td, seed * 1000 + j)
             n = a.numel() * (2 if td == torch.complex64 else 1)
             sites.append(_ops.scale(a, 1.0 / np.sqrt(n)))
-        inputs.append(sites)
+        inputs[i] = sites
         if (d, td) not in idents:
             idents[(d, td)] = _ops.to_device(np.eye(d).reshape(d, d, 1, 1), td)
     torch.cuda.synchronize()
-    order = sorted(range(len(specs)), key=lambda i: -W.spec_flops(specs[i]))
-    results = [None] * len(specs)
+    small = sorted(range(len(specs)), key=lambda i: W.spec_flops(specs[i]))
+    sample = set(small[:6] + small[len(small) // 4: len(small) // 4 + 2])
+    outputs = {}
 
-    def job(i):
+    def make_job(i):
         def f():
             N, d, chi, dt, _ = specs[i]
             st = E.SweepStats()
             out = E.apply_compress_native(inputs[i], [idents[(d, tdt[dt])]] * N, chi // 2, stats=st)
-            results[i] = (st.log_norm, st.bonds, out if i in sample else None)
+            if i in sample:
+                outputs[i] = out
+            return {"log_norm": st.log_norm, "bonds": list(st.bonds)}
         return f
 
-    small = sorted(range(len(specs)), key=lambda i: W.spec_flops(specs[i]))
-    sample = set(small[:6] + small[len(small) // 4: len(small) // 4 + 2])
     B = args.batch
     streams = [torch.cuda.Stream() for _ in range(B)]
-    E.run_queue([job(i) for i in order[:B]], B, streams=streams, stagger=STAGGER)   # warm-up
+
+    def run_jobs(jobs):
+        return E.run_queue(jobs, B, streams=streams, stagger=STAGGER)
+
+    warm = sorted(mine, key=lambda i: -W.spec_flops(specs[i]))[:B]
+    run_jobs([make_job(i) for i in warm])   # warm-up
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+    with ClockSampler(local_rank) as clk:
         torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
         e0.record()
-        E.run_queue([job(i) for i in order], B, streams=streams, stagger=STAGGER)
+        local = W.run_sharded(specs, make_job, run_jobs, rank, world)
         e1.record()
         torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
     elapsed = e0.elapsed_time(e1) / 1e3
-    # parity and CPU baseline on the sample
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    # parity on the sample instances this rank ran
     import tn_oracle as O
-    fid_err, cpu_s = 0.0, 0.0
-    for i in sorted(sample):
+    fid_err, cpu_s, checked = 0.0, 0.0, 0
+    for i in sorted(sample & mine):
         N, d, chi, dt, _ = specs[i]
         host = [a.cpu().numpy().astype(np.complex128 if dt == np.complex64 else np.float64) for a in inputs[i]]
         t0 = time.perf_counter()
         ref = O.svd_compress_method(O.left_canonical_form_mps(host), chi // 2)
         cpu_s += time.perf_counter() - t0
-        got = [o.cpu().numpy().astype(np.complex128) for o in results[i][2]]
+        got = [o.cpu().numpy().astype(np.complex128) for o in outputs[i]]
         fid_err = max(fid_err, 1 - O.fidelity(ref, got))
-    ratio = sum(W.spec_flops(specs[i]) for i in sample) / sum(W.spec_flops(sp) for sp in specs)
-    cpu_rate = len(specs) * ratio / cpu_s if cpu_s > 0 else None
-    line = {"metric": "uneven-batch instances/s (left-canonise + svd_compress to chi/2 + norm; N 16-128, "
-                      "d 2-4, chi 16-256)",
-            "value": len(specs) / elapsed, "unit": "instances/s", "n_gpus": 1, "steps": 1, "warmup": 1,
-            "ms_per_step": elapsed * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32/c64", "data": "synthetic (seeded Gaussian MPS generated on the device)",
-            "config": {"workload": "uneven_batch", "instances": len(specs), "seed": 1, "streams": B,
-                       "scheduling": "heaviest first on a work queue, workers admitted %d ms apart"
-                                     % int(STAGGER * 1e3)},
-            "fidelity_error_max_vs_oracle": fid_err, "oracle_sample": len(sample),
-            "clocks": clk.summary(),
-            "cpu_baseline": {"value": cpu_rate, "unit": "instances/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": "%d instances of the batch through the oracle (left_canonical_form + "
-                                       "svd_compress), scaled by their flop share %.4f" % (len(sample), ratio)}}
-    print(json.dumps(line), flush=True)
+        checked += 1
+    merged = W.gather_results(local, world)
+    if world > 1:
+        stats = [None] * world if rank == 0 else None
+        dist.gather_object((fid_err, cpu_s, checked), stats, dst=0)
+        if rank == 0:
+            fid_err = max(s[0] for s in stats)
+            checked = sum(s[2] for s in stats)
+    if rank == 0:
+        assert merged is not None and sorted(merged) == list(range(len(specs)))
+        ratio_local = sum(W.spec_flops(specs[i]) for i in sample & mine) / sum(W.spec_flops(sp) for sp in specs)
+        cpu_rate = len(specs) * ratio_local / cpu_s if cpu_s > 0 else None
+        line = {"metric": "uneven-batch instances/s (left-canonise + svd_compress to chi/2 + norm; N 16-128, "
+                          "d 2-4, chi 16-256)",
+                "value": len(specs) / elapsed, "unit": "instances/s", "n_gpus": world, "steps": 1, "warmup": 1,
+                "ms_per_step": elapsed * 1e3, "higher_is_better": True, "scaling": "strong",
+                "vs_baseline": None, "dtype": "f32/c64", "data": "synthetic (seeded Gaussian MPS generated on the "
+                                                                  "device)",
+                "config": {"workload": "uneven_batch", "instances": len(specs), "seed": 1, "streams": B,
+                           "parallelism": "flop-partitioned instances over %d rank(s), per-instance scalars "
+                                          "gathered to rank 0" % world,
+                           "scheduling": "heaviest first on a work queue, workers admitted %d ms apart"
+                                         % int(STAGGER * 1e3)},
+                "instances_gathered": len(merged),
+                "fidelity_error_max_vs_oracle": fid_err, "oracle_sample": checked,
+                "clocks": clk.summary(),
+                "cpu_baseline": {"value": cpu_rate, "unit": "instances/s", "cores": os.cpu_count(),
+                                 "kind": "port",
+                                 "sample": "rank 0's instances of the oracle sample through the oracle "
+                                           "(left_canonical_form + svd_compress), scaled by their flop share %.4f"
+                                           % ratio_local}}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
     return 0
 
 

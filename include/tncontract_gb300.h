@@ -53,6 +53,23 @@ enum { TNC_OP_N = 0, TNC_OP_T = 1, TNC_OP_C = 2 /* conj-transpose */, TNC_OP_R =
 
 int tnc_abi_version(void);
 const char *tnc_status_string(int status);
+
+/* Polls every bounded device-side wait makes before it gives up and records
+ * TNC_ERR_TIMEOUT (grid barriers, step counters and flags of the persistent
+ * factorisation kernels; twice as many for the tensor-core GEMM's mbarrier
+ * waits).  Applies to the current device; polls <= 0 restores the default
+ * (2^24, a few seconds).  No counterpart in the reference (which has no
+ * device code); it lets a test make a wait run out. */
+int tnc_set_spin_limit(long long polls);
+/* One CTA waits on something nothing completes -- kind 0: a grid barrier
+ * expecting two CTAs, 1: a step counter nobody publishes, 2: a flag nobody
+ * sets -- until the wait limit runs out; info[0] (device int) receives the
+ * error word, TNC_ERR_TIMEOUT when the bounded wait gave up as designed.
+ * work: 256 bytes of device memory.  A self-test of the failure path the
+ * factorisations share; the reference's counterpart of that path is
+ * tensor_svd's retry and re-raise (tncontract/tensor.py:914-929). */
+int tnc_wait_selftest(int kind, void *work, size_t work_bytes, int *info,
+                      void *stream);
 /* Kernels launched by this library since it was loaded (host counter). */
 unsigned long long tnc_kernel_launches(void);
 
@@ -130,6 +147,29 @@ int tnc_gemm(int dtype, int opA, int opB, int64_t m, int64_t n, int64_t k,
              const void *B, int64_t ldb, int64_t strideB, const double *beta,
              void *C, int64_t ldc, int64_t strideC, int64_t batch,
              void *stream);
+
+/* Up to TNC_GEMM_GROUP_MAX independent products of different shapes in one
+ * launch (CUDA-core tiles, round-to-nearest FMA): problem i computes
+ * C_i = alpha_i op(A_i) op(B_i) + beta_i C_i on row-major operands as
+ * tnc_gemm does (k >= 1; problems with m or n = 0 are skipped).  `problems`
+ * is a HOST array.  The independent pairwise contractions of one network
+ * (con's cost-ordered plan) run as one grouped launch per wave; in the
+ * reference they are successive np.tensordot calls in tncontract/tncon.py:
+ * 131-155. */
+#define TNC_GEMM_GROUP_MAX 16
+typedef struct {
+  int opA, opB;
+  int64_t m, n, k;
+  const void *A;
+  int64_t lda;
+  const void *B;
+  int64_t ldb;
+  void *C;
+  int64_t ldc;
+  double alpha[2], beta[2];
+} tnc_gemm_problem;
+int tnc_gemm_grouped(int dtype, int count, const tnc_gemm_problem *problems,
+                     void *stream);
 
 /* tnc_gemm on the tcgen05 tensor cores for F32 / C64: TF32 split products
  * (hi*hi + hi*lo + lo*hi, FP32 accumulation in tensor memory) give
@@ -209,11 +249,15 @@ int tnc_svd(int dtype, int64_t m, int64_t n, const void *A, int64_t lda,
  * framework that owns the whole device-memory budget, a service that
  * reserves all memory at start-up).  The work area is a fixed 16 MiB
  * array inside the library image (held by every GPU that loads the library
- * until exit); problems whose tnc_svd_workspace_size exceeds it return
- * TNC_ERR_TOO_LARGE.  Same arguments and results as tnc_svd otherwise.  All
- * calls on a device share that area: calls that overlap on the GPU race, so
- * order them on one stream.  The first call on a device looks up the area's
- * device address (with that device current); make it before any stream
+ * until exit); a problem is accepted when tnc_svd_workspace_size(dtype, m, n)
+ * is at most 16 MiB (e.g. complex128 up to 450 x 450 or 433 x 512, complex64
+ * and float64 up to 647 x 647 or 531 x 1024), otherwise TNC_ERR_TOO_LARGE is
+ * returned before anything is launched or written.  Same arguments and
+ * results as tnc_svd otherwise.  All calls on a device share that area:
+ * calls that overlap on the GPU race, so order them on one stream.  The
+ * area's device address is looked up (with the device current) on the first
+ * call on a device, and again after that device's context was destroyed and
+ * re-created (cudaDeviceReset); make those calls before any stream
  * capture. */
 int tnc_svd_noalloc(int dtype, int64_t m, int64_t n, const void *A,
                     int64_t lda, void *U, void *S, void *VH, int max_sweeps,

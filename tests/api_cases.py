@@ -478,3 +478,26 @@ def check_onedim_edges(tn, tol=1e-10):
     assert close(np.transpose(full, [0, 2, 1, 3]), g["e_Tmpo"], tol)
     assert _raises_name(lambda: oc.tensor_to_mpo(T, physout_labels=["o1"], physin_labels=["i1", "i2"])) \
         == m["e_t2o_mismatch"]
+
+
+def con_fixture_network(tn, name):
+    """Tensors and pairs of one of the reference's con fixture networks."""
+    g, m = load("con_cases")
+    tensors = [tn.Tensor(g["%s_in%d" % (name, i)], labels) for i, labels in enumerate(m[name + "_in_labels"])]
+    return tensors, [tuple(p) for p in m[name + "_pairs"]], g[name + "_out"], m[name + "_out_labels"]
+
+
+def con_waves(tn, tensors, pairs):
+    """The waves of con's cost-ordered plan for a network (host only)."""
+    from tncontract_gb300 import tncon
+    labels = [list(t.labels) for t in tensors]
+    index_lookup = tncon._index_lookup(labels, pairs)
+    internal, _pw = tncon._group_pairs(pairs, index_lookup)
+    traced = tncon._traced_labels(labels, internal, index_lookup)
+    shapes = [[dict(zip(lb, t.shape))[l] for l in tl] for t, lb, tl in zip(tensors, labels, traced)]
+    partner = {}
+    for c in pairs:
+        if index_lookup[c[0]] != index_lookup[c[1]]:
+            partner[c[0]], partner[c[1]] = c[1], c[0]
+    steps, _ = tncon._greedy_plan(shapes, traced, partner)
+    return tncon.plan_waves(steps)

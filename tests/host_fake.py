@@ -193,7 +193,12 @@ def _adam_step(p, g, m, v, lr, b1, b2, eps, step):
     p.sub_(lr * (m / (1 - b1 ** step)) / (torch.sqrt(v / (1 - b2 ** step)) + eps))
 
 
+def _tensordot_many(items):
+    return [_tensordot(a, b, aa, ab) for a, b, aa, ab in items]
+
+
 PATCH = {
+    "tensordot_many": _tensordot_many,
     "fill_gaussian": _fill_gaussian,
     "dense_forward": _dense_forward,
     "dense_backward": _dense_backward,

@@ -88,3 +88,26 @@ def test_con_order_argument_validation():
             tn.con(A, B, ("y", "z"), order="fastest")
         with pytest.raises(ValueError):
             tn.con(A, B, ("y", "z"), ("y", "w"))
+
+
+def test_con_waves_of_independent_pairs():
+    """The cost-ordered plan of the reference's 2x3 grid network (breadth-first pair order) has a wave
+    of two or more independent merges (one grouped GEMM launch on the
+    device); waves touch disjoint nodes and keep every merge once; the values
+    stay the reference's (CPU stand-in)."""
+    import tncontract_gb300 as tn
+    from tncontract_gb300 import tncon
+    with cpu_ops():
+        tensors, pairs, want, want_labels = K.con_fixture_network(tn, "grid_2x3_bfs")
+    waves = K.con_waves(tn, tensors, pairs)
+    assert max(len(w) for w in waves) >= 2
+    for w in waves:
+        touched = [n for st in w for n in st[:2]]
+        assert len(touched) == len(set(touched))
+    assert sum(len(w) for w in waves) == len(tensors) - 1
+    # a chain whose two end pairs are independent: [[A.B, C.D], [AB.CD]]
+    steps = [(0, 1, ["a"], ["b"]), (2, 3, ["c"], ["d"]), (0, 2, ["x"], ["y"])]
+    assert [[s[:2] for s in w] for w in tncon.plan_waves(steps)] == [[(0, 1), (2, 3)], [(0, 2)]]
+    with cpu_ops():
+        r = tn.con(tensors, pairs)
+    assert r.labels == want_labels and K.close(r.to_numpy(), want, 1e-12)

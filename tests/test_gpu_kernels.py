@@ -295,3 +295,59 @@ def test_gemm_tensor_core(gpu, dt):
         ref = ref.real
     assert relerr(host(Cd), ref) < 3e-5
     assert _lib.lib().tnc_gemm_tc_error() == 0
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64, np.complex64, np.complex128])
+def test_gemm_grouped(gpu, dt):
+    """tnc_gemm_grouped: independent products of different shapes and
+    operand layouts in one launch, each against NumPy."""
+    from tncontract_gb300 import _lib as L
+    from tncontract_gb300 import _ops
+    rng = np.random.default_rng(12)
+    cplx = np.iscomplexobj(np.zeros(0, dt))
+
+    def rnd(*shape):
+        a = rng.standard_normal(shape)
+        if cplx:
+            a = a + 1j * rng.standard_normal(shape)
+        return a.astype(dt)
+    ops = {L.OP_N: lambda x: x, L.OP_T: lambda x: x.T, L.OP_C: lambda x: np.conj(x).T, L.OP_R: np.conj}
+    cases = [(L.OP_N, L.OP_N, 70, 33, 129), (L.OP_T, L.OP_N, 5, 200, 17), (L.OP_N, L.OP_C, 64, 64, 64),
+             (L.OP_C, L.OP_T, 130, 1, 300), (L.OP_R, L.OP_N, 1, 7, 3)]
+    probs, want = [], []
+    for opA, opB, m, n, k in cases:
+        A = rnd(*((k, m) if opA in (L.OP_T, L.OP_C) else (m, k)))
+        B = rnd(*((n, k) if opB in (L.OP_T, L.OP_C) else (k, n)))
+        Cm = torch.empty((m, n), dtype=torch.from_numpy(A).dtype, device="cuda")
+        probs.append((opA, opB, m, n, k, torch.from_numpy(A).cuda(), A.shape[1], torch.from_numpy(B).cuda(),
+                      B.shape[1], Cm, n))
+        want.append(ops[opA](A.astype(np.complex128)) @ ops[opB](B.astype(np.complex128)))
+    before = L.kernel_launches()
+    _ops.gemm_grouped(probs)
+    torch.cuda.synchronize()
+    assert L.kernel_launches() - before == 1
+    tol = 1e-5 if dt in (np.float32, np.complex64) else 1e-12
+    for p, w in zip(probs, want):
+        assert np.linalg.norm(p[9].cpu().numpy() - w) <= tol * np.linalg.norm(w) + 1e-30
+
+
+def test_con_wave_is_one_launch(gpu):
+    """con's cost-ordered plan on the reference's 2x3 grid network issues one
+    grouped GEMM launch per wave of independent pairwise contractions (no
+    single-product GEMM), and the result is the reference's."""
+    import api_cases as K
+    import tncontract_gb300 as tn
+    from tncontract_gb300 import _ops
+    tensors, pairs, want, want_labels = K.con_fixture_network(tn, "grid_2x3_bfs")
+    waves = K.con_waves(tn, tensors, pairs)
+    assert max(len(w) for w in waves) >= 2
+    _ops.PROFILE = {}
+    try:
+        r = tn.con(tensors, pairs)
+        torch.cuda.synchronize()
+        prof = _ops.PROFILE
+    finally:
+        _ops.PROFILE = None
+    assert len(prof.get("tnc_gemm_grouped", [])) == len(waves)
+    assert "tnc_gemm" not in prof and "tnc_gemm_tc" not in prof
+    assert r.labels == want_labels and K.close(r.to_numpy(), want, 1e-12)

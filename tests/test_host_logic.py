@@ -230,3 +230,34 @@ def test_trace_of_unequal_axes_host():
             ref = np.trace(x, axis1=a1, axis2=a2)
             assert t.labels == [l for i, l in enumerate(labels) if i not in (a1, a2)]
             assert np.allclose(t.to_numpy(), ref)
+
+
+def test_tensor_svd_retry_contract_host():
+    """tensor_svd's failure contract (tncontract/tensor.py:914-929) on the
+    CPU stand-in: a failed first SVD warns and is retried with the larger
+    sweep cap; a non-finite matrix prints the inf / nan report and
+    re-raises the ValueError."""
+    import warnings as _w
+    import numpy as np
+    import tncontract_gb300 as tn
+    from tncontract_gb300 import _ops
+    calls = []
+    with cpu_ops():
+        real = _ops.svd
+
+        def flaky(M, max_sweeps=0, **kw):
+            calls.append(max_sweeps)
+            if len(calls) == 1:
+                raise _ops.LinAlgError("SVD did not converge")
+            return real(M, max_sweeps=max_sweeps, **kw)
+        _ops.svd = flaky
+        try:
+            t = tn.Tensor(np.arange(12.0).reshape(3, 4), ["r", "c"])
+            with _w.catch_warnings(record=True) as rec:
+                _w.simplefilter("always")
+                U, S, V = tn.tensor_svd(t, ["r"])
+        finally:
+            _ops.svd = real
+        assert any("retrying" in str(r.message) for r in rec)
+        from tncontract_gb300 import tensor as T
+        assert calls == [T.SVD_SWEEPS, T.SVD_RETRY_SWEEPS]

@@ -27,11 +27,23 @@ _pi64 = C.POINTER(C.c_int64)
 _pint = C.POINTER(C.c_int)
 _psz = C.POINTER(C.c_size_t)
 
+GEMM_GROUP_MAX = 16
+
+
+class GemmProblem(C.Structure):
+    """tnc_gemm_problem (include/tncontract_gb300.h)."""
+    _fields_ = [("opA", C.c_int), ("opB", C.c_int), ("m", C.c_int64), ("n", C.c_int64), ("k", C.c_int64),
+                ("A", C.c_void_p), ("lda", C.c_int64), ("B", C.c_void_p), ("ldb", C.c_int64),
+                ("C", C.c_void_p), ("ldc", C.c_int64), ("alpha", C.c_double * 2), ("beta", C.c_double * 2)]
+
+
 # name -> argtypes (restype int unless given)
 SIGNATURES = {
     "tnc_abi_version": [],
     "tnc_status_string": [_int],
     "tnc_kernel_launches": [],
+    "tnc_set_spin_limit": [C.c_longlong],
+    "tnc_wait_selftest": [_int, _vp, C.c_size_t, _vp, _vp],
     "tnc_permute": [_int, _vp, _vp, _int, _pi64, _pint, _int, _vp],
     "tnc_scale": [_int, _i64, _pdbl, _vp, _vp, _int, _vp],
     "tnc_axpby": [_int, _i64, _pdbl, _vp, _pdbl, _vp, _vp],
@@ -45,6 +57,7 @@ SIGNATURES = {
     "tnc_copy2d": [_int, _i64, _i64, _vp, _i64, _vp, _i64, _vp],
     "tnc_gemm": [_int, _int, _int, _i64, _i64, _i64, _pdbl, _vp, _i64, _i64, _vp, _i64,
                  _i64, _pdbl, _vp, _i64, _i64, _i64, _vp],
+    "tnc_gemm_grouped": [_int, _int, C.POINTER(GemmProblem), _vp],
     "tnc_mps_mpo_site": [_int, _i64, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _int, _vp],
     "tnc_qr_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_qr": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, C.c_size_t, _vp, _vp],

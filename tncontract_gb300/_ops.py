@@ -472,6 +472,72 @@ def tensordot(a, b, axes_a, axes_b):
     return out
 
 
+def _tensordot_prepare(a, b, axes_a, axes_b):
+    """Operands of np.tensordot(a, b, (axes_a, axes_b)) as one GEMM: at most
+    one permute per operand.  Returns (out, gemm arguments or None)."""
+    axes_a = [int(x) % a.dim() for x in axes_a] if a.dim() else []
+    axes_b = [int(x) % b.dim() for x in axes_b] if b.dim() else []
+    dt = torch.promote_types(a.dtype, b.dtype)
+    a = cast(a.contiguous(), dt)
+    b = cast(b.contiguous(), dt)
+    free_a = [i for i in range(a.dim()) if i not in axes_a]
+    free_b = [i for i in range(b.dim()) if i not in axes_b]
+    ma = int(np.prod([a.shape[i] for i in free_a], dtype=np.int64))
+    nb = int(np.prod([b.shape[i] for i in free_b], dtype=np.int64))
+    kk = int(np.prod([a.shape[i] for i in axes_a], dtype=np.int64))
+    out = empty([a.shape[i] for i in free_a] + [b.shape[i] for i in free_b], dt)
+    if ma == 0 or nb == 0:
+        return out, None
+    if free_a + axes_a == list(range(a.dim())):
+        opA, Am, lda = L.OP_N, a, kk
+    elif axes_a + free_a == list(range(a.dim())):
+        opA, Am, lda = L.OP_T, a, ma
+    else:
+        opA, Am, lda = L.OP_N, permute(a, free_a + axes_a), kk
+    if axes_b + free_b == list(range(b.dim())):
+        opB, Bm, ldb = L.OP_N, b, nb
+    elif free_b + axes_b == list(range(b.dim())):
+        opB, Bm, ldb = L.OP_T, b, kk
+    else:
+        opB, Bm, ldb = L.OP_N, permute(b, axes_b + free_b), nb
+    return out, (opA, opB, ma, nb, kk, Am, max(lda, 1), Bm, max(ldb, 1), out, nb)
+
+
+def gemm_grouped(problems):
+    """Independent products (opA, opB, m, n, k, A, lda, B, ldb, C, ldc) of
+    one dtype, C = op(A) op(B), as one launch per TNC_GEMM_GROUP_MAX of them
+    (``tnc_gemm_grouped``)."""
+    if not problems:
+        return
+    dt = code(problems[0][9].dtype)
+    for i in range(0, len(problems), L.GEMM_GROUP_MAX):
+        chunk = problems[i:i + L.GEMM_GROUP_MAX]
+        arr = (L.GemmProblem * len(chunk))()
+        flops = 0.0
+        for slot, (opA, opB, m, n, k, A, lda, B, ldb, Cm, ldc) in zip(arr, chunk):
+            slot.opA, slot.opB, slot.m, slot.n, slot.k = opA, opB, m, n, k
+            slot.A, slot.lda, slot.B, slot.ldb, slot.C, slot.ldc = A.data_ptr(), lda, B.data_ptr(), ldb, \
+                Cm.data_ptr(), ldc
+            slot.alpha[0], slot.alpha[1], slot.beta[0], slot.beta[1] = 1.0, 0.0, 0.0, 0.0
+            flops += 2.0 * m * n * k * (4 if is_complex(Cm.dtype) else 1)
+        _call("tnc_gemm_grouped", dt, len(chunk), arr, _stream(), flops=flops)
+
+
+def tensordot_many(items):
+    """np.tensordot for several independent (a, b, axes_a, axes_b): operand
+    permutes where needed, then the products of each dtype as one grouped
+    GEMM launch.  Returns the results in order."""
+    outs, by_dtype = [], {}
+    for a, b, axes_a, axes_b in items:
+        out, g = _tensordot_prepare(a, b, axes_a, axes_b)
+        outs.append(out)
+        if g is not None:
+            by_dtype.setdefault(out.dtype, []).append(g)
+    for probs in by_dtype.values():
+        gemm_grouped(probs)
+    return outs
+
+
 def mps_mpo_site(A, W, layout):
     """Fused MPO-MPS site product; A (din, chl, chr), W (dout, din, Dl, Dr)."""
     din, chl, chr_ = A.shape
@@ -488,6 +554,22 @@ def mps_mpo_site(A, W, layout):
 
 
 # ------------------------------------------------------------------ factorisations
+
+
+def set_spin_limit(polls=0):
+    """Polls every bounded device-side wait makes before giving up
+    (``tnc_set_spin_limit``; 0 restores the default), current device."""
+    _call("tnc_set_spin_limit", int(polls))
+
+
+def wait_selftest(kind):
+    """Run one CTA whose bounded wait nothing completes (0 grid barrier,
+    1 step counter, 2 flag) and return its error word (``TNC_ERR_TIMEOUT``
+    when the wait gave up as designed)."""
+    ws = workspace(256)
+    info = torch.zeros(1, dtype=torch.int32, device=device())
+    _call("tnc_wait_selftest", int(kind), _p(ws), 256, _p(info), _stream())
+    return int(info[0].item())
 
 
 def svd(M, max_sweeps=0, tol=0.0, check=True, info_out=None):

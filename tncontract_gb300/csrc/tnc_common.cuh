@@ -13,6 +13,16 @@
 
 namespace tnc {
 
+// Default poll count of every bounded device-side wait (tnc_persist.cuh and the
+// tensor-core GEMM's mbarrier waits); tnc_set_spin_limit changes it at run time.
+constexpr long long kSpinLimitDefault = 1LL << 24;
+// Per-translation-unit setters of the wait limit on the current device (each
+// unit that spins keeps its own device copy of the limit).
+int spin_limit_set_qr(long long polls);
+int spin_limit_set_svd(long long polls);
+int spin_limit_set_rows(long long polls);
+int spin_limit_set_tc(long long polls);
+
 // ---------------------------------------------------------------- complex
 template <typename R>
 struct __align__(2 * sizeof(R)) cplx {

@@ -78,76 +78,150 @@ __device__ __forceinline__ void tile_store(T* s, const T (&v)[GemmTile<T>::PER],
   }
 }
 
+// One 64 x 64 output tile (rows m0.., columns n0..) of C = alpha op(A) op(B) + beta C.
+template <typename T, bool AK, bool BKM>
+__device__ __forceinline__ void gemm_tile(int64_t M, int64_t N, int64_t K, bool aC, bool bC, T alpha,
+                                          const T* __restrict__ Ab, int64_t lda, const T* __restrict__ Bb,
+                                          int64_t ldb, T beta, T* __restrict__ Cb, int64_t ldc, int64_t m0,
+                                          int64_t n0, T (*As)[GemmTile<T>::BK * GemmTile<T>::LD],
+                                          T (*Bs)[GemmTile<T>::BK * GemmTile<T>::LD]) {
+  typedef GemmTile<T> G;
+  constexpr int TM = 4, TN = 4;
+  const int tid = threadIdx.x;
+  const int tx = tid % (G::BN / TN), ty = tid / (G::BN / TN);
+  const bool beta_zero = (abs2_(beta) == 0);
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = zero_<T>();
+
+  T va[G::PER], vb[G::PER];
+  tile_fetch<T, AK>(Ab, lda, m0, M, 0, K, va);
+  tile_fetch<T, BKM>(Bb, ldb, n0, N, 0, K, vb);
+  tile_store<T, AK>(As[0], va, aC);
+  tile_store<T, BKM>(Bs[0], vb, bC);
+  __syncthreads();
+  int buf = 0;
+  for (int64_t k0 = 0; k0 < K; k0 += G::BK) {
+    const bool more = k0 + G::BK < K;
+    if (more) {
+      tile_fetch<T, AK>(Ab, lda, m0, M, k0 + G::BK, K, va);
+      tile_fetch<T, BKM>(Bb, ldb, n0, N, k0 + G::BK, K, vb);
+    }
+    const T* as = As[buf];
+    const T* bs = Bs[buf];
+#pragma unroll
+    for (int kk = 0; kk < G::BK; ++kk) {
+      T a[TM], b[TN];
+      lds4(as + kk * G::LD + ty * TM, a);
+      lds4(bs + kk * G::LD + tx * TN, b);
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) fma_(acc[i][j], a[i], b[j]);
+    }
+    if (more) {
+      tile_store<T, AK>(As[buf ^ 1], va, aC);
+      tile_store<T, BKM>(Bs[buf ^ 1], vb, bC);
+    }
+    __syncthreads();
+    buf ^= 1;
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int64_t gm = m0 + ty * TM + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int64_t gn = n0 + tx * TN + j;
+      if (gn >= N) continue;
+      T v = alpha * acc[i][j];
+      if (!beta_zero) v += beta * Cb[gm * ldc + gn];
+      Cb[gm * ldc + gn] = v;
+    }
+  }
+}
+
 template <typename T, bool AK, bool BKM>
 __global__ void __launch_bounds__(256)
 gemm_simt_kernel(int64_t M, int64_t N, int64_t K, bool aC, bool bC, T alpha, const T* __restrict__ A, int64_t lda,
                  int64_t sA, const T* __restrict__ B, int64_t ldb, int64_t sB, T beta, T* __restrict__ C,
                  int64_t ldc, int64_t sC, int64_t batch) {
   typedef GemmTile<T> G;
-  constexpr int TM = 4, TN = 4;
   __shared__ __align__(16) T As[2][G::BK * G::LD];
   __shared__ __align__(16) T Bs[2][G::BK * G::LD];
-  const int tid = threadIdx.x;
-  const int tx = tid % (G::BN / TN), ty = tid / (G::BN / TN);
   const int64_t m0 = (int64_t)blockIdx.y * G::BM, n0 = (int64_t)blockIdx.x * G::BN;
-  const bool beta_zero = (abs2_(beta) == 0);
-
   for (int64_t bz = blockIdx.z; bz < batch; bz += gridDim.z) {
-    const T* Ab = A + bz * sA;
-    const T* Bb = B + bz * sB;
-    T* Cb = C + bz * sC;
-    T acc[TM][TN];
-#pragma unroll
-    for (int i = 0; i < TM; ++i)
-#pragma unroll
-      for (int j = 0; j < TN; ++j) acc[i][j] = zero_<T>();
-
-    T va[G::PER], vb[G::PER];
-    tile_fetch<T, AK>(Ab, lda, m0, M, 0, K, va);
-    tile_fetch<T, BKM>(Bb, ldb, n0, N, 0, K, vb);
-    tile_store<T, AK>(As[0], va, aC);
-    tile_store<T, BKM>(Bs[0], vb, bC);
-    __syncthreads();
-    int buf = 0;
-    for (int64_t k0 = 0; k0 < K; k0 += G::BK) {
-      const bool more = k0 + G::BK < K;
-      if (more) {
-        tile_fetch<T, AK>(Ab, lda, m0, M, k0 + G::BK, K, va);
-        tile_fetch<T, BKM>(Bb, ldb, n0, N, k0 + G::BK, K, vb);
-      }
-      const T* as = As[buf];
-      const T* bs = Bs[buf];
-#pragma unroll
-      for (int kk = 0; kk < G::BK; ++kk) {
-        T a[TM], b[TN];
-        lds4(as + kk * G::LD + ty * TM, a);
-        lds4(bs + kk * G::LD + tx * TN, b);
-#pragma unroll
-        for (int i = 0; i < TM; ++i)
-#pragma unroll
-          for (int j = 0; j < TN; ++j) fma_(acc[i][j], a[i], b[j]);
-      }
-      if (more) {
-        tile_store<T, AK>(As[buf ^ 1], va, aC);
-        tile_store<T, BKM>(Bs[buf ^ 1], vb, bC);
-      }
-      __syncthreads();
-      buf ^= 1;
-    }
-#pragma unroll
-    for (int i = 0; i < TM; ++i) {
-      const int64_t gm = m0 + ty * TM + i;
-      if (gm >= M) continue;
-#pragma unroll
-      for (int j = 0; j < TN; ++j) {
-        const int64_t gn = n0 + tx * TN + j;
-        if (gn >= N) continue;
-        T v = alpha * acc[i][j];
-        if (!beta_zero) v += beta * Cb[gm * ldc + gn];
-        Cb[gm * ldc + gn] = v;
-      }
-    }
+    gemm_tile<T, AK, BKM>(M, N, K, aC, bC, alpha, A + bz * sA, lda, B + bz * sB, ldb, beta, C + bz * sC, ldc, m0,
+                          n0, As, Bs);
+    __syncthreads();  // the next batch entry reuses the shared tiles
   }
+}
+
+// Independent products of different shapes in one launch: the CTAs of the
+// grid are dealt out to the problems' output tiles (problem q owns tiles
+// [tile0_q, tile0_{q+1})), each problem with its own operand layouts.
+struct GroupProblem {
+  int64_t m, n, k, lda, ldb, ldc, tile0, tiles_n;
+  const void* A;
+  const void* B;
+  void* C;
+  double alpha[2], beta[2];
+  int opA, opB;
+};
+constexpr int kGroupMax = 16;
+struct GemmGroup {
+  int count;
+  GroupProblem p[kGroupMax];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_grouped_kernel(const __grid_constant__ GemmGroup g) {
+  typedef GemmTile<T> G;
+  __shared__ __align__(16) T As[2][G::BK * G::LD];
+  __shared__ __align__(16) T Bs[2][G::BK * G::LD];
+  int q = 0;
+  while (q + 1 < g.count && (int64_t)blockIdx.x >= g.p[q + 1].tile0) ++q;
+  const GroupProblem& P = g.p[q];
+  const int64_t t = (int64_t)blockIdx.x - P.tile0;
+  const int64_t m0 = (t / P.tiles_n) * G::BM, n0 = (t % P.tiles_n) * G::BN;
+  const T alpha = from_pair<T>(P.alpha), beta = from_pair<T>(P.beta);
+  const bool aK = (P.opA == TNC_OP_N || P.opA == TNC_OP_R), bK = (P.opB == TNC_OP_T || P.opB == TNC_OP_C);
+  const bool aC = (P.opA == TNC_OP_C || P.opA == TNC_OP_R), bC = (P.opB == TNC_OP_C || P.opB == TNC_OP_R);
+  const T* A = (const T*)P.A;
+  const T* B = (const T*)P.B;
+  T* C = (T*)P.C;
+  if (aK && bK) gemm_tile<T, true, true>(P.m, P.n, P.k, aC, bC, alpha, A, P.lda, B, P.ldb, beta, C, P.ldc, m0, n0, As, Bs);
+  else if (aK) gemm_tile<T, true, false>(P.m, P.n, P.k, aC, bC, alpha, A, P.lda, B, P.ldb, beta, C, P.ldc, m0, n0, As, Bs);
+  else if (bK) gemm_tile<T, false, true>(P.m, P.n, P.k, aC, bC, alpha, A, P.lda, B, P.ldb, beta, C, P.ldc, m0, n0, As, Bs);
+  else gemm_tile<T, false, false>(P.m, P.n, P.k, aC, bC, alpha, A, P.lda, B, P.ldb, beta, C, P.ldc, m0, n0, As, Bs);
+}
+
+template <typename T>
+int gemm_grouped_launch(int count, const tnc_gemm_problem* probs, cudaStream_t st) {
+  if (count <= 0 || count > kGroupMax || !probs) return TNC_ERR_ARG;
+  GemmGroup g;
+  g.count = 0;
+  int64_t tiles = 0;
+  for (int i = 0; i < count; ++i) {
+    const tnc_gemm_problem& p = probs[i];
+    if (p.m < 0 || p.n < 0 || p.k <= 0 || p.opA < 0 || p.opA > 3 || p.opB < 0 || p.opB > 3 || p.ldc < p.n)
+      return TNC_ERR_ARG;
+    if (p.m == 0 || p.n == 0) continue;
+    if (!p.A || !p.B || !p.C) return TNC_ERR_ARG;
+    GroupProblem& q = g.p[g.count++];
+    q.m = p.m; q.n = p.n; q.k = p.k; q.lda = p.lda; q.ldb = p.ldb; q.ldc = p.ldc;
+    q.A = p.A; q.B = p.B; q.C = p.C; q.opA = p.opA; q.opB = p.opB;
+    q.alpha[0] = p.alpha[0]; q.alpha[1] = p.alpha[1]; q.beta[0] = p.beta[0]; q.beta[1] = p.beta[1];
+    q.tiles_n = (p.n + GemmTile<T>::BN - 1) / GemmTile<T>::BN;
+    q.tile0 = tiles;
+    tiles += q.tiles_n * ((p.m + GemmTile<T>::BM - 1) / GemmTile<T>::BM);
+  }
+  if (g.count == 0) return TNC_OK;
+  if (tiles > 0x7fffffff) return TNC_ERR_ARG;
+  gemm_grouped_kernel<T><<<(unsigned)tiles, 256, 0, st>>>(g);
+  return launch_status();
 }
 
 // C = beta*C when K == 0 (np.tensordot over no axes still has the outer
@@ -220,5 +294,11 @@ extern "C" int tnc_gemm(int dtype, int opA, int opB, int64_t m, int64_t n, int64
                return gemm_launch<T>(opA, opB, m, n, k, from_pair<T>(alpha), (const T*)A, lda, strideA,
                                      (const T*)B, ldb, strideB, from_pair<T>(beta), (T*)C, ldc, strideC, batch,
                                      st));
+  return TNC_ERR_ARG;
+}
+
+extern "C" int tnc_gemm_grouped(int dtype, int count, const tnc_gemm_problem* problems, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  TNC_DISPATCH(dtype, T, return gemm_grouped_launch<T>(count, problems, st));
   return TNC_ERR_ARG;
 }

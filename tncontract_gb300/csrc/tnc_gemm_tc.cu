@@ -35,9 +35,16 @@ namespace tnc {
 
 constexpr int kTcBM = 128;                 // tile rows (UMMA M)
 constexpr int kTcBK = 32;                  // K elements per stage = one 128-byte swizzle atom of FP32
-constexpr long long kTcSpin = 1LL << 25;   // mbarrier polls before giving up
+// mbarrier polls before giving up: twice the library's wait limit
+// (tnc_set_spin_limit), a try_wait poll being shorter than a sleeping one
+static __device__ long long g_tc_spin = 2 * kSpinLimitDefault;
 
 __device__ int g_tc_error = 0;
+
+int spin_limit_set_tc(long long polls) {
+  const long long v = 2 * polls;
+  return cudaMemcpyToSymbol(g_tc_spin, &v, sizeof(v)) == cudaSuccess ? TNC_OK : TNC_ERR_CUDA;
+}
 
 // ------------------------------------------------------------------ PTX wrappers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -64,8 +71,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   long long spins = 0;
+  const long long limit = *(volatile long long*)&g_tc_spin;
   while (!mbar_try_wait(bar, parity)) {
-    if (++spins > kTcSpin) {
+    if (++spins > limit) {
       atomicExch(&g_tc_error, 1);
       return false;
     }

@@ -9,9 +9,21 @@
 
 namespace tnc {
 
-// Roughly 2-4 s of polling at ~150 ns per iteration: orders of magnitude above
-// any legitimate wait (one Jacobi round or one Householder column step).
-constexpr long long kSpinLimit = 1LL << 24;
+// Polls a bounded wait makes before it gives up.  The default, roughly 2-4 s of
+// polling at ~150 ns per iteration, is orders of magnitude above any
+// legitimate wait (one Jacobi round or one Householder column step).  The
+// value is a device variable of every translation unit that includes this
+// header, set for the current device by tnc_set_spin_limit (tests shorten it
+// to make a wait run out on purpose).
+static __device__ long long g_spin_limit = kSpinLimitDefault;
+__device__ __forceinline__ long long spin_limit() { return *(volatile long long*)&g_spin_limit; }
+
+// Host side: sets this translation unit's copy on the current device.
+#define TNC_DEFINE_SPIN_SETTER(name)                                                         \
+  int name(long long polls) {                                                                \
+    return cudaMemcpyToSymbol(g_spin_limit, &polls, sizeof(polls)) == cudaSuccess ? TNC_OK \
+                                                                                   : TNC_ERR_CUDA; \
+  }
 
 struct SyncWords {
   unsigned count;  // grid barrier arrivals; the top bit is the phase
@@ -42,9 +54,10 @@ __device__ __forceinline__ bool grid_barrier(SyncWords* sw, unsigned nblocks) {
     // the CTA whose arrival flips the phase bit completed the barrier
     const bool last = (((old + add) ^ old) & 0x80000000u) != 0;
     long long spins = 0;
+    const long long limit = spin_limit();
     while (!last && ((ld_volatile(&sw->count) ^ old) & 0x80000000u) == 0) {
       if (ld_volatile(&sw->err)) { ok = 0; break; }
-      if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
+      if (++spins > limit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
       __nanosleep(32);
     }
     __threadfence();
@@ -59,9 +72,10 @@ __device__ __forceinline__ bool warp_wait_flag(const int* flag, SyncWords* sw) {
   int ok = 1;
   if ((threadIdx.x & 31) == 0) {
     long long spins = 0;
+    const long long limit = spin_limit();
     while (ld_volatile(flag) == 0) {
       if (ld_volatile(&sw->err)) { ok = 0; break; }
-      if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
+      if (++spins > limit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
       __nanosleep(32);
     }
     __threadfence();

@@ -921,6 +921,8 @@ template int qr_qt<double>(int64_t, int64_t, const double*, int, bool, double*, 
 template int qr_qt<c64>(int64_t, int64_t, const c64*, int, bool, c64*, void*, size_t, int*, cudaStream_t, c64**);
 template int qr_qt<c128>(int64_t, int64_t, const c128*, int, bool, c128*, void*, size_t, int*, cudaStream_t, c128**);
 
+TNC_DEFINE_SPIN_SETTER(spin_limit_set_qr)
+
 }  // namespace tnc
 
 using namespace tnc;

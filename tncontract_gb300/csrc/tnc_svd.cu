@@ -263,6 +263,8 @@ static int svd_impl(int64_t m, int64_t n, const T* A, int64_t lda, T* U, typenam
   return gemm_launch<T>(TNC_OP_N, TNC_OP_R, nr, L, nr, one, small, nr, 0, Qt, L, 0, zero, VH, L, 0, 1, st);
 }
 
+TNC_DEFINE_SPIN_SETTER(spin_limit_set_svd)
+
 }  // namespace tnc
 
 using namespace tnc;
@@ -295,10 +297,11 @@ extern "C" int tnc_svd(int dtype, int64_t m, int64_t n, const void* A, int64_t l
 // __device__ array): every GPU that loads the library holds these bytes until
 // the process exits, and no call allocates or frees device memory.
 //
-// Limit: the problem's workspace (tnc_svd_workspace_size) must fit in
-// kNoAllocScratchBytes = 16 MiB, e.g. complex128 up to 448 x 512 or
-// complex64 up to 512 x 1024; larger problems are rejected with
-// TNC_ERR_TOO_LARGE before anything is launched.
+// Limit: a problem is accepted when its workspace, tnc_svd_workspace_size(
+// dtype, m, n), fits in kNoAllocScratchBytes = 16 MiB: e.g. complex128 up to
+// 450 x 450 or 433 x 512, complex64 / float64 up to 647 x 647 or 531 x 1024,
+// float32 up to 931 x 931 (either orientation).  Larger problems are rejected
+// with TNC_ERR_TOO_LARGE before anything is launched or written.
 //
 // All calls on a device share the one scratch area and it keeps whatever the
 // previous call left there; the SVD initialises every part it reads (working
@@ -307,10 +310,16 @@ extern "C" int tnc_svd(int dtype, int64_t m, int64_t n, const void* A, int64_t l
 // different host threads without ordering) race on the shared scratch: order
 // them on one stream.
 //
-// The device address of the scratch is looked up once per device, with that
-// device current, on the first call made on it (cudaGetSymbolAddress); make
-// that first call before any stream capture.
+// The device address of the scratch is looked up with the device current
+// (cudaGetSymbolAddress) on the first call made on a device, and looked up
+// again when that device's context is no longer the one the address was
+// taken in (after cudaDeviceReset, or a primary context released and
+// re-created, the library image is loaded anew at another address); make the
+// first call on a device, and the first after such a reset, before any
+// stream capture.
 // ---------------------------------------------------------------------------
+#include <cuda.h>
+
 #include <mutex>
 
 namespace tnc {
@@ -318,20 +327,46 @@ namespace tnc {
 static constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_svd_scratch[kNoAllocScratchBytes];
 
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+
+// cuCtxGetCurrent through the runtime's driver entry point (no link-time
+// dependency on the driver library)
+static CtxGetCurrentFn ctx_get_current() {
+  static std::once_flag once;
+  static CtxGetCurrentFn fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  });
+  return fn;
+}
+
+struct NoallocSlot {
+  CUcontext ctx;  // the context the address was looked up in
+  void* ptr;
+};
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[128] = {nullptr};  // device address per device ordinal
+static NoallocSlot g_noalloc[128] = {};  // per device ordinal
 
 static int noalloc_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TNC_ERR_CUDA;
   if (dev < 0 || dev >= 128) return TNC_ERR_ARG;
+  CtxGetCurrentFn get = ctx_get_current();
+  if (!get) return TNC_ERR_CUDA;
+  CUcontext ctx = nullptr;
+  if (get(&ctx) != CUDA_SUCCESS) return TNC_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (g_noalloc_ptr[dev] == nullptr) {
-    void* p = nullptr;
+  if (ctx == nullptr || g_noalloc[dev].ptr == nullptr || g_noalloc[dev].ctx != ctx) {
+    void* p = nullptr;  // the lookup also makes the device's primary context current
     if (cudaGetSymbolAddress(&p, g_noalloc_svd_scratch) != cudaSuccess || p == nullptr) return TNC_ERR_CUDA;
-    g_noalloc_ptr[dev] = p;
+    if (get(&ctx) != CUDA_SUCCESS || ctx == nullptr) return TNC_ERR_CUDA;
+    g_noalloc[dev] = NoallocSlot{ctx, p};
   }
-  *out = g_noalloc_ptr[dev];
+  *out = g_noalloc[dev].ptr;
   return TNC_OK;
 }
 

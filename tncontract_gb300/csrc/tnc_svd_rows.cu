@@ -196,11 +196,12 @@ __device__ __forceinline__ bool wait_steps(const unsigned* ver, int64_t P, int64
   if (threadIdx.x == 0) {
     int ok = 1;
     long long spins = 0;
+    const long long limit = spin_limit();
     for (;;) {
       const unsigned a = ld_volatile(ver + P), b = ld_volatile(ver + Q);
       if (a >= target && b >= target) break;
       if (ld_volatile(&sw->err)) { ok = 0; break; }
-      if (++spins > kSpinLimit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
+      if (++spins > limit) { atomicCAS(&sw->err, 0, TNC_ERR_TIMEOUT); ok = 0; break; }
       __nanosleep(32);
     }
     __threadfence();
@@ -383,6 +384,22 @@ __global__ void gather_rows_kernel(const T* src, int64_t L, const int64_t* order
   }
 }
 
+// Self-test of the bounded waits: one CTA waits on something nothing will
+// complete -- a grid barrier expecting two CTAs (kind 0), a half-block step
+// counter nobody publishes (kind 1), a flag nobody sets (kind 2) -- until the
+// wait limit runs out, then reports the error word (TNC_ERR_TIMEOUT).
+__global__ void wait_selftest_kernel(int kind, SyncWords* sw, unsigned* ver, int* flag, int* info) {
+  if (kind == 0) {
+    grid_barrier(sw, 2u);
+  } else if (kind == 1) {
+    wait_steps(ver, 0, 1, 1u, sw);
+  } else if (threadIdx.x < 32) {
+    warp_wait_flag(flag, sw);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) info[0] = ld_volatile(&sw->err);
+}
+
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct RowsLayout { size_t d, dn, frob2, counters, sync, total; };
@@ -535,6 +552,8 @@ static int gather_impl(const T* src, int64_t L, const int64_t* order, const int6
   return launch_status();
 }
 
+TNC_DEFINE_SPIN_SETTER(spin_limit_set_rows)
+
 }  // namespace tnc
 
 using namespace tnc;
@@ -563,4 +582,25 @@ extern "C" int tnc_gather_rows(int dtype, const void* src, int64_t L, const int6
                return gather_impl<T>((const T*)src, L, order, k, kmax, (const typename traits<T>::real*)S, mode,
                                      (T*)dst, st));
   return TNC_ERR_ARG;
+}
+
+extern "C" int tnc_set_spin_limit(long long polls) {
+  if (polls <= 0) polls = kSpinLimitDefault;
+  if (int rc = spin_limit_set_qr(polls)) return rc;
+  if (int rc = spin_limit_set_svd(polls)) return rc;
+  if (int rc = spin_limit_set_rows(polls)) return rc;
+  return spin_limit_set_tc(polls);
+}
+
+extern "C" int tnc_wait_selftest(int kind, void* work, size_t work_bytes, int* info, void* stream) {
+  if (kind < 0 || kind > 2 || !work || !info || work_bytes < 256) return TNC_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = (char*)work;
+  SyncWords* sw = (SyncWords*)w;
+  unsigned* ver = (unsigned*)(w + 64);
+  int* flag = (int*)(w + 128);
+  if (cudaMemsetAsync(work, 0, 256, st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(info, 0, sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
+  wait_selftest_kernel<<<1, 64, 0, st>>>(kind, sw, ver, flag, info);
+  return launch_status(1);
 }

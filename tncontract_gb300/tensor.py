@@ -16,6 +16,7 @@ returns the discarded singular values as a device tensor.
 from __future__ import annotations
 
 import copy as _copy
+import warnings
 
 import numpy as np
 import torch
@@ -459,6 +460,29 @@ def contract(tensor1, tensor2, labels1, labels2, index_slice1=None, index_slice2
     ``index_slice`` selects a subset (``-1`` = last).  The result's labels are
     the uncontracted labels of ``tensor1`` then ``tensor2`` in their original
     order.  Mismatches raise the reference's ``ValueError`` diagnostics."""
+    ax1, ax2 = _contract_axes(tensor1, tensor2, labels1, labels2, index_slice1, index_slice2)
+    data = _ops.tensordot(tensor1.data, tensor2.data, ax1, ax2)
+    return _contract_result(tensor1, tensor2, ax1, ax2, data)
+
+
+def contract_many(jobs):
+    """Several independent ``contract(t1, t2, labels1, labels2)`` calls (no
+    tensor shared between them): labels resolved and checked on the host one
+    by one, then every product issued as one grouped GEMM launch
+    (``_ops.tensordot_many``).  Returns the results in order."""
+    axes = [_contract_axes(t1, t2, l1, l2, None, None) for t1, t2, l1, l2 in jobs]
+    datas = _ops.tensordot_many([(t1.data, t2.data, a1, a2) for (t1, t2, _l1, _l2), (a1, a2) in zip(jobs, axes)])
+    return [_contract_result(t1, t2, a1, a2, d) for (t1, t2, _l1, _l2), (a1, a2), d in zip(jobs, axes, datas)]
+
+
+def _contract_result(tensor1, tensor2, ax1, ax2, data):
+    new1 = [l for j, l in enumerate(tensor1.labels) if j not in ax1]
+    new2 = [l for j, l in enumerate(tensor2.labels) if j not in ax2]
+    return _new(data, new1 + new2)
+
+
+def _contract_axes(tensor1, tensor2, labels1, labels2, index_slice1, index_slice2):
+    """Axes of ``contract``, with the reference's diagnostics on mismatch."""
     labels1, labels2, ax1, ax2 = _resolve(tensor1, tensor2, labels1, labels2,
                                           index_slice1, index_slice2)
     ok = len(ax1) == len(ax2) and all(
@@ -479,10 +503,7 @@ def contract(tensor1, tensor2, labels1, labels2, index_slice1=None, index_slice2
             if not labels2[i] in tensor2.labels:
                 raise ValueError(labels2[i] + ' not in list of labels for tensor2')
         raise ValueError("shape-mismatch for sum")
-    data = _ops.tensordot(tensor1.data, tensor2.data, ax1, ax2)
-    new1 = [l for j, l in enumerate(tensor1.labels) if j not in ax1]
-    new2 = [l for j, l in enumerate(tensor2.labels) if j not in ax2]
-    return _new(data, new1 + new2)
+    return ax1, ax2
 
 
 def tensor_product(*args):
@@ -544,10 +565,36 @@ def _matricise(tensor, row_labels):
     return data.reshape(nrow, ncol), shape, ax.labels
 
 
+# Sweep caps of the drop-in SVD: the first attempt (0 = the kernel's default,
+# 40) and the retry after a non-convergence.  The reference retries a failed
+# np.linalg.svd (gesdd) once with scipy's gesvd driver (tensor.py:914-929);
+# here the retry is the same Jacobi with a larger sweep cap.
+SVD_SWEEPS = 0
+SVD_RETRY_SWEEPS = 100
+
+
+def _svd_checked(mat):
+    """``np.linalg.svd(full_matrices=False)`` with the reference's failure
+    contract (tensor.py:914-929): on a failure, warn and retry once; if the
+    retry fails on non-finite input, print whether the matrix holds inf's /
+    nan's and re-raise (ValueError); a retry that does not converge raises
+    LinAlgError."""
+    try:
+        return _ops.svd(mat, max_sweeps=SVD_SWEEPS)
+    except (_ops.LinAlgError, ValueError):
+        warnings.warn("tensor_svd: the Jacobi SVD failed, retrying with %d sweeps" % SVD_RETRY_SWEEPS)
+        try:
+            return _ops.svd(mat, max_sweeps=SVD_RETRY_SWEEPS)
+        except ValueError:
+            print("tensor_svd failed. Matrix contains inf's: " + str(bool(torch.isinf(mat).any().item()))
+                  + ". Matrix contains nan's: " + str(bool(torch.isnan(mat).any().item())))
+            raise
+
+
 def _svd_parts(tensor, row_labels, svd_label):
     mat, old_shape, labels = _matricise(tensor, row_labels)
     column_labels = [x for x in labels if x not in row_labels]
-    u, s, v = _ops.svd(mat)
+    u, s, v = _svd_checked(mat)
     U = _new(u.reshape(tuple(old_shape[:len(row_labels)]) + (u.shape[1],)),
              list(row_labels) + [svd_label + "in"])
     V = _new(v.reshape((v.shape[0],) + tuple(old_shape[len(row_labels):])),

@@ -210,6 +210,25 @@ def _greedy_plan(shapes, labels, partner):
     return steps, total
 
 
+def plan_waves(steps):
+    """Group a merge list [(i, j, ...)] (node j absorbed into node i) into
+    waves of independent merges: a merge goes one wave after the last merge
+    that wrote either of its nodes, so the merges of a wave touch disjoint
+    nodes and can run together (one grouped GEMM launch).  Order inside a
+    wave and of the waves follows the plan."""
+    level = {}
+    waves = []
+    for st in steps:
+        i, j = st[0], st[1]
+        w = max(level.get(i, -1), level.get(j, -1)) + 1
+        level[i] = w
+        level[j] = w
+        if w == len(waves):
+            waves.append([])
+        waves[w].append(st)
+    return waves
+
+
 def _argument_cost(shapes, labels, internal_contract, pairwise_contract, index_lookup):
     """Multiply-adds of the reference's argument order (for comparison)."""
     dims = {}
@@ -300,9 +319,11 @@ def con(*args, order="cost"):
             partner[c[0]], partner[c[1]] = c[1], c[0]
     steps, _ = _greedy_plan([t.shape for t in tensor_list], [list(t.labels) for t in tensor_list], partner)
     nodes = {i: t for i, t in enumerate(tensor_list)}
-    for i, j, la, lb in steps:
-        nodes[i] = tn.contract(nodes[i], nodes[j], la, lb)
-        del nodes[j]
+    for wave in plan_waves(steps):
+        results = tn.contract_many([(nodes[i], nodes[j], la, lb) for i, j, la, lb in wave])
+        for (i, j, _la, _lb), r in zip(wave, results):
+            nodes[i] = r
+            del nodes[j]
     result = tn.tensor_product(*[nodes[i] for i in sorted(nodes)])
     if result.labels != ref_labels:
         perm = [result.labels.index(l) for l in ref_labels]

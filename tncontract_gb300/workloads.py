@@ -184,3 +184,34 @@ def partition_by_flops(specs, world):
         parts[r].append(i)
         load[r] += cost[i]
     return [sorted(p) for p in parts]
+
+
+def run_sharded(specs, make_job, run_jobs, rank=0, world=1):
+    """Run this rank's share of independent instances: the flop-balanced
+    split of ``partition_by_flops`` (every rank computes the same split, so
+    no data moves between ranks), heaviest first.  ``make_job(i)`` returns a
+    callable computing instance i's result; ``run_jobs(jobs)`` runs a list of
+    them (on the GPU: ``engine.run_queue`` over worker streams) and returns
+    their results in order.  Returns {instance index: result} for this rank."""
+    mine = partition_by_flops(specs, world)[rank]
+    mine = sorted(mine, key=lambda i: (-spec_flops(specs[i]), i))
+    results = run_jobs([make_job(i) for i in mine])
+    return dict(zip(mine, results))
+
+
+def gather_results(local, world, dst=0):
+    """The only exchange of a sharded batch: every rank's {index: per-instance
+    scalars} gathered to rank ``dst`` (torch.distributed.gather_object over
+    the default process group).  Returns the merged dict on ``dst``, None on
+    the other ranks; with one rank, ``local`` itself."""
+    if world <= 1:
+        return local
+    import torch.distributed as dist
+    got = [None] * world if dist.get_rank() == dst else None
+    dist.gather_object(local, got, dst=dst)
+    if dist.get_rank() != dst:
+        return None
+    merged = {}
+    for part in got:
+        merged.update(part)
+    return merged
