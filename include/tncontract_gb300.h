@@ -307,10 +307,13 @@ int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
  * precision; TNC_CORE_FP64 (1, F32 / C64 storage only) finishes the Jacobi of
  * each core (rows up to 512 for C64, 1024 for F32) in FP64 after the
  * storage-precision Jacobi, and takes the singular values, the truncation
- * decision and U from the FP64 rows.  core_tol: that FP64 Jacobi's
- * tolerance (<= 0: 1e-8, pairs of rows orthogonal to 1e-8 relative; U is
- * stored back in single precision and the singular values' error is second
- * order in it).  The core changes the workspace size.
+ * decision and U from the FP64 rows (the storage-precision stage then runs
+ * to 3e-6 and at most 14 sweeps, a stall above that handing over to the FP64
+ * stage).  core_tol: the FP64 stage's tolerance (<= 0: 1e-7, pairs of rows
+ * orthogonal to 1e-7 relative, the rounding level of U's single-precision
+ * storage; the singular values' error from it is second order).  The
+ * singular values inherit the storage-precision stage's rounding (FP32-class
+ * relative to s_max).  The core changes the workspace size.
  * out_discarded (HOST, may be NULL): n_sites-1 doubles, [i] = the fraction of
  * the squared singular values discarded at the bond between sites i and i+1.
  * *log_norm: in, the natural log of the input state's norm factor; out, that

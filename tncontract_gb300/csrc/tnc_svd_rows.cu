@@ -217,19 +217,26 @@ __device__ __forceinline__ bool wait_steps(const unsigned* ver, int64_t P, int64
 // so two CTAs fit on one SM: the kernel is latency-bound (8 warps, dependent
 // rotation steps), and concurrent factorisations on other streams fill the
 // second slot.  The bound costs a few spilled registers.
-template <typename T, int MAXE, int MAXT>
+// FP64 rows (PREG = false) keep both half-blocks in shared memory and the
+// kernel at 128 registers: its rotations are bound by the FP64 pipe (1.6 FMA a
+// clock per SM on GB300, measured), not by shared-memory traffic, and the other
+// half of the register file stays free for an FP32 kernel of another instance
+// on the same SM (a register-resident FP64 row took all 255 registers a
+// thread, so nothing else could share the SM).
+template <typename T, int MAXE, int MAXT, bool PREG>
 constexpr int jacobi_min_blocks() {
-  return (MAXT == 256 && MAXE <= 16 && sizeof(typename traits<T>::real) == 4) ? 2 : 1;
+  return (!PREG || (MAXT == 256 && MAXE <= 16 && sizeof(typename traits<T>::real) == 4)) ? 2 : 1;
 }
 
-template <typename T, int MAXE, int MAXT>
-__global__ void __launch_bounds__(MAXT, jacobi_min_blocks<T, MAXE, MAXT>())
+template <typename T, int MAXE, int MAXT, bool PREG>
+__global__ void __launch_bounds__(MAXT, jacobi_min_blocks<T, MAXE, MAXT, PREG>())
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
                     typename traits<T>::real* Dn, unsigned* counters, unsigned* ver, SyncWords* sw, int* info) {
   typedef typename traits<T>::real R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sB = reinterpret_cast<T*>(smem_raw);
-  __shared__ R sn[32];  // squared norms of the shared-memory rows
+  __shared__ R sn[32];   // squared norms of the shared-memory rows
+  __shared__ R snA[32];  // ... of the P half-block when it is in shared memory too
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nb = (nr + h - 1) / h;
   const int64_t nbp = nb + (nb & 1);
@@ -239,7 +246,7 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
   int sweep = 0;
   bool converged = false;
   unsigned last_rot = 0;
-  T x[MAXE];
+  T x[PREG ? MAXE : 1];
   for (; sweep < max_sweeps; ++sweep) {
     unsigned rot = 0;
     // step index of this sweep's phase 0; a sweep is nbp steps (phase 0 and
@@ -286,38 +293,62 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
           continue;
         }
         if (!wait_steps(ver, P, Q, g, sw)) return;
-        const int64_t rowA = P * h + warp;
-        const bool hasA = rowA < nr;
         const int64_t q0 = Q * h;
         const int cntB = (int)((nr - q0) < h ? (nr - q0) : h);
-        R an = 0;
-        if (hasA) {
+        if constexpr (PREG) {
+          const int64_t rowA = P * h + warp;
+          const bool hasA = rowA < nr;
+          R an = 0;
+          if (hasA) {
 #pragma unroll
-          for (int u = 0; u < MAXE; ++u) {
-            const int64_t k = lane + 32 * u;
-            x[u] = (k < L) ? ldcg(W + rowA * L + k) : zero_<T>();
+            for (int u = 0; u < MAXE; ++u) {
+              const int64_t k = lane + 32 * u;
+              x[u] = (k < L) ? ldcg(W + rowA * L + k) : zero_<T>();
+            }
+            an = ldcg(Dn + rowA);
           }
-          an = ldcg(Dn + rowA);
-        }
-        rows_to_smem(W, q0, cntB, L, sB);
-        if (threadIdx.x < cntB) sn[threadIdx.x] = ldcg(Dn + q0 + threadIdx.x);
-        __syncthreads();
-        for (int s = 0; s < h; ++s) {
-          const int j = (warp + s) % h;
-          if (hasA && j < cntB)
-            rot += rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol, noise2, an, &sn[j]) ? 1u : 0u;
+          rows_to_smem(W, q0, cntB, L, sB);
+          if (threadIdx.x < cntB) sn[threadIdx.x] = ldcg(Dn + q0 + threadIdx.x);
           __syncthreads();
-        }
-        if (hasA) {
-#pragma unroll
-          for (int u = 0; u < MAXE; ++u) {
-            const int64_t k = lane + 32 * u;
-            if (k < L) stcg(W + rowA * L + k, x[u]);
+          for (int s = 0; s < h; ++s) {
+            const int j = (warp + s) % h;
+            if (hasA && j < cntB)
+              rot += rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol, noise2, an, &sn[j]) ? 1u : 0u;
+            __syncthreads();
           }
-          if (lane == 0) stcg(Dn + rowA, an);
+          if (hasA) {
+#pragma unroll
+            for (int u = 0; u < MAXE; ++u) {
+              const int64_t k = lane + 32 * u;
+              if (k < L) stcg(W + rowA * L + k, x[u]);
+            }
+            if (lane == 0) stcg(Dn + rowA, an);
+          }
+          rows_from_smem(W, q0, cntB, L, sB);
+          if (threadIdx.x < cntB) stcg(Dn + q0 + threadIdx.x, sn[threadIdx.x]);
+        } else {
+          T* sA = sB + (int64_t)h * L;
+          const int64_t p0 = P * h;
+          const int cntA = (int)((nr - p0) < h ? (nr - p0) : h);
+          rows_to_smem(W, p0, cntA, L, sA);
+          rows_to_smem(W, q0, cntB, L, sB);
+          if (threadIdx.x < cntA) snA[threadIdx.x] = ldcg(Dn + p0 + threadIdx.x);
+          if (threadIdx.x < cntB) sn[threadIdx.x] = ldcg(Dn + q0 + threadIdx.x);
+          __syncthreads();
+          for (int s = 0; s < h; ++s) {
+            const int j = (warp + s) % h;
+            if (warp < cntA && j < cntB)
+              rot += rotate_smem_smem(sA + (int64_t)warp * L, sB + (int64_t)j * L, L, rtol, noise2, &snA[warp],
+                                      &sn[j])
+                         ? 1u
+                         : 0u;
+            __syncthreads();
+          }
+          rows_from_smem(W, p0, cntA, L, sA);
+          if (threadIdx.x < cntA) stcg(Dn + p0 + threadIdx.x, snA[threadIdx.x]);
+          rows_from_smem(W, q0, cntB, L, sB);
+          if (threadIdx.x < cntB) stcg(Dn + q0 + threadIdx.x, sn[threadIdx.x]);
         }
-        rows_from_smem(W, q0, cntB, L, sB);
-        if (threadIdx.x < cntB) stcg(Dn + q0 + threadIdx.x, sn[threadIdx.x]);
         publish_steps(ver, P, Q, g + 1u);
       }
     }
@@ -428,27 +459,27 @@ template <> int dtype_code<c128>() { return TNC_C128; }
 // different row lengths share the setting).
 static const size_t kMaxHalfBlockBytes = 200 * 1024;
 
-template <typename T, int MAXE, int MAXT>
+template <typename T, int MAXE, int MAXT, bool PREG>
 static int ensure_smem_attr() {
   static std::atomic<unsigned long long> done_mask{0};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return TNC_ERR_CUDA;
   const unsigned long long bit = 1ull << (dev & 63);
   if (done_mask.load() & bit) return TNC_OK;
-  if (cudaFuncSetAttribute((const void*)jacobi_block_kernel<T, MAXE, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)kMaxHalfBlockBytes) != cudaSuccess)
+  if (cudaFuncSetAttribute((const void*)jacobi_block_kernel<T, MAXE, MAXT, PREG>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxHalfBlockBytes) != cudaSuccess)
     return TNC_ERR_CUDA;
   done_mask.fetch_or(bit);
   return TNC_OK;
 }
 
-template <typename T, int MAXE, int MAXT>
+template <typename T, int MAXE, int MAXT, bool PREG = true>
 static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, const double* frob2,
                         typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info, cudaStream_t st) {
-  const size_t smem = (size_t)h * L * sizeof(T);
-  const void* fn = (const void*)jacobi_block_kernel<T, MAXE, MAXT>;
+  const size_t smem = (size_t)(PREG ? 1 : 2) * h * L * sizeof(T);
+  const void* fn = (const void*)jacobi_block_kernel<T, MAXE, MAXT, PREG>;
   if (smem > kMaxHalfBlockBytes || 32 * h > MAXT) return TNC_ERR_ARG;
-  if (int rc = ensure_smem_attr<T, MAXE, MAXT>()) return rc;
+  if (int rc = ensure_smem_attr<T, MAXE, MAXT, PREG>()) return rc;
   const int threads = 32 * h;
   int cap = coop_capacity(fn, threads, smem);
   if (cap <= 0) return TNC_ERR_CUDA;
@@ -517,7 +548,12 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
     while (h > 2 && h / 2 >= nr) h >>= 1;
     const bool big = sizeof(T) >= 16;
     int rc;
-    if (h == 16) {
+    if (sizeof(typename traits<T>::real) == 8 && L <= 512) {
+      // FP64 rows: both half-blocks in shared memory (2 h L elements)
+      if (h > 8) h = 8;
+      while (h > 2 && (size_t)2 * h * L * sizeof(T) > kMaxHalfBlockBytes) h >>= 1;
+      rc = launch_block<T, 1, 256, false>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+    } else if (h == 16) {
       if constexpr (sizeof(T) <= 8) {
         if (L <= 256) rc = launch_block<T, 8, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
         else rc = launch_block<T, 16, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);

@@ -25,9 +25,8 @@
 // With the FP64 core (core = 1, single-precision storage only) the Jacobi of
 // every truncating bond runs twice: the storage-precision Jacobi above brings
 // the rows of R to orthogonality at the FP32 rounding level, then the rows are
-// widened to FP64 and a one-sided FP64 Jacobi finishes them (from a start that
-// close, one rotating sweep and one checking sweep at the default tolerance
-// kCoreTol);
+// widened to FP64 and a one-sided FP64 Jacobi finishes them (tolerances
+// kCoreFp32Tol / kCoreTol: usually one rotating and one checking FP64 sweep);
 // the singular values, the truncation decision (s / s_max > threshold, at most
 // chi) and U come from the FP64 rows.  The products around the core stay in
 // the storage precision.
@@ -61,12 +60,20 @@ struct Dims {
   bool core64 = false;      // FP64 Jacobi finish of the bond cores
 };
 
-// Default tolerance of the FP64 finish: |<w_i, w_j>| <= tol |w_i| |w_j| for every
-// pair of rows.  U is stored back in single precision, so orthogonality below
-// the FP32 rounding level is not kept, and the singular values' error is second
-// order in the tolerance (1e-16 relative at 1e-8): from the FP32-converged
-// start (pairs at ~1e-5) one rotating sweep and one checking sweep suffice.
-constexpr double kCoreTol = 1e-8;
+// Tolerances of the two Jacobi stages of an FP64 core (|<w_i, w_j>| <= tol
+// |w_i| |w_j| for every pair of rows).  The FP32 stage runs to 3e-6, near its
+// rounding floor (sqrt(L) eps_32 ~ 2.7e-6 at L = 512), and at most
+// kCoreFp32Sweeps sweeps: a stage that stalls above the tolerance is not an
+// error, the FP64 stage takes over from where it stopped.  The FP64 stage
+// runs to 1e-7: U is stored back in single precision, whose rounding (6e-8
+// per entry) already limits its orthogonality to that level, and the
+// singular values' error from the tolerance is second order (1e-14).  From
+// that start one rotating FP64 sweep and one checking sweep usually suffice
+// (measured at 512 x 512: 2 FP64 sweeps, against 3 with an FP32 stage at its
+// default 1.1e-5 and an FP64 stage at 1e-8).
+constexpr double kCoreFp32Tol = 3e-6;
+constexpr int kCoreFp32Sweeps = 14;
+constexpr double kCoreTol = 1e-7;
 
 // the FP64 type that finishes the Jacobi of a single-precision core
 inline int core_dtype(int dt) { return dt == TNC_C64 ? TNC_C128 : TNC_F64; }
@@ -361,10 +368,11 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
     prof.add(1, qr_flops(n, m, cplx));
     const bool rows_path = m <= rows_limit(dt);
     prof.begin(2, st);
+    const bool core_path = P.core64 && rows_path && m <= core_rows_limit(dt);
     if (rows_path) {
       if (tnc_svd_rows_workspace_size(dt, kmin, m, &xb) != TNC_OK || xb > factb) return TNC_ERR_WORKSPACE;
-      if (int rc = tnc_svd_rows(dt, kmin, m, B.rbuf, B.wbuf, B.S, B.order, 0, 0.0, block_rows, B.fact, factb, B.info,
-                                st))
+      if (int rc = tnc_svd_rows(dt, kmin, m, B.rbuf, B.wbuf, B.S, B.order, core_path ? kCoreFp32Sweeps : 0,
+                                core_path ? kCoreFp32Tol : 0.0, block_rows, B.fact, factb, B.info, st))
         return rc;
     } else {  // the accumulating SVD of R: its VH rows are U^H of M
       if (tnc_svd_workspace_size(dt, kmin, m, &xb) != TNC_OK || xb > factb) return TNC_ERR_WORKSPACE;
@@ -373,9 +381,9 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
     }
     prof.end(2, st);
     // the FP64 finish of the core (rows up to the FP64 register limit)
-    const bool core_path = P.core64 && rows_path && m <= core_rows_limit(dt);
     if (core_path) {
-      if (int stq = device_status(B.info, st)) return stq;
+      // an FP32 stage that stopped at its sweep cap hands over to the FP64 stage
+      if (int stq = device_status(B.info, st); stq && stq != TNC_ERR_NOT_CONVERGED) return stq;
       prof.add(2, svd_flops(kmin, m, cplx));
       const int cdt = core_dtype(dt);
       if (int rc = tnc_cast(dt, cdt, kmin * m, B.wbuf, B.w64a, st)) return rc;
