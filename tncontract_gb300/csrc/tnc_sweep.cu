@@ -89,14 +89,14 @@ size_t tc_ws(int dt, int64_t m, int64_t n, int64_t k, int64_t batch) {
   return b;
 }
 
-// The sweep's absorption products run on the CUDA-core GEMM (round-to-nearest
-// FMA).  The tensor cores' FP32 accumulation truncates toward zero, which
-// biases every product's magnitude down by ~1e-8 x K: over the 190 products
-// of a sweep at chi = 256 that shrank the state's norm by 1.6e-3 (its
-// direction, and so the fidelity, was unaffected).
+// The sweep's absorption products of single-precision sites run on the
+// tensor-core GEMM, whose error-free digit split keeps the products unbiased
+// (a TF32 split accumulated with truncation in tensor memory had shrunk the
+// state's norm by 1.6e-3 over the 190 products of a chi = 256 sweep); small
+// products stay on the CUDA-core GEMM.
 bool use_tc(int dt, int64_t m, int64_t n, int64_t k, int64_t batch) {
-  (void)dt, (void)m, (void)n, (void)k, (void)batch;
-  return false;
+  return fp32_class(dt) && (m < n ? m : n) >= 64 && k >= 32 && (double)m * n * k * batch >= (double)(1 << 21) &&
+         batch <= 65535;
 }
 
 int64_t rows_limit(int dt) { return fp32_class(dt) ? 1024 : 512; }
