@@ -61,8 +61,9 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 engine arm")
     p.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the plain FP64 engine arm")
-    p.add_argument("--workload", default="tfim", choices=["tfim", "uneven"],
-                   help="tfim: the headline sweep; uneven: the uneven batch of independent MPS")
+    p.add_argument("--workload", default="tfim", choices=["tfim", "uneven", "learned"],
+                   help="tfim: the headline sweep; uneven: the uneven batch of independent MPS; learned: "
+                        "config 5 (XXZ D=5, N=128, chi=512, learned rank against the plain and FP64 sweeps)")
     p.add_argument("--instances", type=int, default=512, help="instances of the uneven batch")
     p.add_argument("--micro", default=None,
                    help="time one native op instead: svd:MxN:DT, qr:MxN:DT or gemm:MxNxK:DT "
@@ -631,12 +632,77 @@ def run_uneven(args):
     return 0
 
 
+def run_learned(args):
+    """Config 5, learned-rank truncation at full size: a random float32 MPS
+    (N=128, d=2, chi=512, seed 5) under the Heisenberg XXZ MPO (Delta=0.8,
+    D=5), compressed with the discarded-weight rule (tolerance 1e-8, at most
+    chi).  The rank predictor is first trained on the GPU by the library's
+    own MLP kernels on spectra of plain sweeps of configs 1-3
+    (``learned.train_rank_model``); then the sweep runs without it (full SVD
+    at every bond) and with it (randomized SVD sized by the prediction,
+    oversampling 16, 2 power iterations, the full SVD as fallback and judge),
+    and once in FP64 as the reference both are compared with.  One step =
+    one sweep; sweeps/s with and without the predictor, the fallback rate and
+    the fidelity errors are reported."""
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from tncontract_gb300 import engine as E
+    from tncontract_gb300 import learned as LR
+    from tncontract_gb300 import workloads as W
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    N, chi, tol = args.nsites, args.chi, 1e-8
+    t0 = time.perf_counter()
+    model, hist, ntrain = LR.train_rank_model(tol)
+    t_train = time.perf_counter() - t0
+    sites, mpo = LR.config5_inputs(N, 2, chi)
+    LR.config5(sites[:8], mpo[:8], min(chi, 64), tol)          # warm-up (first launches)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        plain, t_plain, rs_plain, st_plain = LR.config5(sites, mpo, chi, tol)
+        learn, t_learn, rs_learn, st_learn = LR.config5(sites, mpo, chi, tol, model=model)
+    f32, t_f32, _rs32, _st32 = LR.config5(sites, mpo, chi, tol, precision="fp32")
+    ref, t_ref, _rs, st_ref = LR.config5(sites, mpo, chi, tol, precision="fp64")
+
+    def fid(a, b):
+        return 1.0 - E.fidelity([x.to(torch.float64) for x in a], [x.to(torch.float64) for x in b])
+    bonds = lambda P: [int(a.shape[2]) for a in P[:-1]]  # noqa: E731
+    flops = W.sweep_flops(N, 2, 5, chi, complex_=False)["total"]
+    line = {"metric": "config 5 learned-rank apply+compress sweeps/s (XXZ D=5, N=%d, chi=%d, float32, "
+                      "discarded weight <= 1e-8)" % (N, chi),
+            "value": 1.0 / t_learn, "unit": "sweeps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": t_learn * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64core", "data": "synthetic (seeded random MPS, XXZ MPO)",
+            "config": {"workload": "config5_learned_rank", "nsites": N, "phys_dim": 2, "mpo_bond": 5, "chi": chi,
+                       "dw_tol": tol, "oversample": 16, "power_iters": 2,
+                       "timing": "one sweep each, host wall clock around a synchronised sweep"},
+            "precision": "mixed (float32 sites and products, FP64 Jacobi finish of every bond core)",
+            "plain_sweeps_per_s": 1.0 / t_plain, "fp64_sweeps_per_s": 1.0 / t_ref,
+            "fp32_core_sweeps_per_s": 1.0 / t_f32, "fidelity_error_fp32_core_vs_fp64": fid(f32, ref),
+            "speedup_learned_vs_plain": t_plain / t_learn,
+            "fallback_rate": LR.fallback_rate(rs_learn), "bonds_sketched": rs_learn.sketched,
+            "bonds_fallback": rs_learn.fallbacks, "bonds_full_svd": rs_learn.full,
+            "bonds_declined_cap_bound": rs_learn.declined,
+            "rows_factored_learned_over_plain": rs_learn.rows_factored / max(rs_plain.rows_factored, 1),
+            "fidelity_error_plain_vs_fp64": fid(plain, ref), "fidelity_error_learned_vs_fp64": fid(learn, ref),
+            "bond_dims_match_fp64": {"plain": bonds(plain) == bonds(ref), "learned": bonds(learn) == bonds(ref)},
+            "training": {"bonds": ntrain, "loss_first": hist[0], "loss_last": hist[-1], "seconds": t_train},
+            "sweep_tflop_fixed_count": flops / 1e12,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.micro:
         return run_micro(args)
     if args.workload == "uneven":
         return run_uneven(args)
+    if args.workload == "learned":
+        if args.nsites == N_SITES and args.chi == CHI:
+            args.nsites, args.chi = 128, 512
+        return run_learned(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -25,8 +25,6 @@ def test_svd_rows(gpu, dt, shape, block_rows):
     from tncontract_gb300 import _ops
     if np.dtype(dt).itemsize * (2 if np.iscomplexobj(np.zeros(0, dt)) else 1) >= 16 and max(shape) > 512:
         pytest.skip("FP64 complex rows above 512 use the accumulating SVD")
-    if np.dtype(dt) == np.float64 and max(shape) > 512:
-        pytest.skip("FP64 rows above 512 use the accumulating SVD")
     rng = np.random.default_rng(11)
     A = rnd(rng, shape, dt)
     W, S, order, info = _ops.svd_rows(torch.from_numpy(A).cuda(), block_rows=block_rows)

@@ -118,7 +118,8 @@ def qr_left_sweep(P):
 
 
 def _rows_limit(dtype):
-    return 512 if dtype in (torch.complex128, torch.float64) else 1024
+    # register-resident rows of the Jacobi: 1024 entries of up to 8 bytes, 512 of complex128
+    return 512 if dtype == torch.complex128 else 1024
 
 
 def _check_info(info):
@@ -129,7 +130,14 @@ def _check_info(info):
         raise _ops.LinAlgError("SVD did not converge (status %d)" % st)
 
 
-def _factor_full(M):
+# FP64 core finish (the "mixed" precision of single-precision sites): the
+# tolerances of the storage-precision Jacobi stage and of the FP64 stage, as
+# in the native sweep (tnc_sweep.cu)
+CORE_FP32_TOL, CORE_FP32_SWEEPS, CORE_FP64_TOL = 3e-6, 14, 1e-7
+_WIDE = {torch.float32: torch.float64, torch.complex64: torch.complex128}
+
+
+def _factor_full(M, core=None):
     """Full SVD of M (m x n) -> (S device, factors(k) -> (U_k, SV_k)).
 
     Columns up to the register limit (m rows) use the QR-preconditioned,
@@ -144,6 +152,23 @@ def _factor_full(M):
     the accumulating SVD on the same R (its VH rows are then U^H of M)."""
     m, n = M.shape
     R = _ops.qr_r(M, adjoint=True)                                         # min(m, n) x m
+    wide = _WIDE.get(M.dtype)
+    if core == "fp64" and wide is not None and m <= _rows_limit(wide):
+        # FP32 Jacobi to near its rounding floor (a stall is handed over), then
+        # the FP64 Jacobi finishes the widened rows; S, the rank decision and U
+        # come from the FP64 rows, U is stored back in the sites' precision
+        W32, _s, _o, info = _ops.svd_rows(R, max_sweeps=CORE_FP32_SWEEPS, tol=CORE_FP32_TOL)
+        if int(info[0].item()) not in (L.OK, L.ERR_NOT_CONVERGED):
+            _check_info(info)
+        W, S, order, info = _ops.svd_rows(_ops.cast(W32, wide), tol=CORE_FP64_TOL)
+        _check_info(info)
+
+        def factors(k, kdev):
+            U = _ops.cast(_ops.gather_rows(W, order, kdev, k, S=S, mode=1), M.dtype)   # m x k
+            SV = _ops.empty((k, n), M.dtype)
+            _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)     # U^H M
+            return U, SV
+        return S, factors
     if m <= _rows_limit(M.dtype):
         W, S, order, info = _ops.svd_rows(R)                               # W rows = S U^H
         _check_info(info)
@@ -164,7 +189,7 @@ def _factor_full(M):
     return S, factors
 
 
-def _factor_sketch(M, l, power_iters, seed):
+def _factor_sketch(M, l, power_iters, seed, core=None):
     """Randomized range finder (Halko, Martinsson & Tropp 2011, alg. 4.4):
     Q = orth((M M^H)^q M Omega) with Omega n x l Gaussian, re-orthonormalised
     after every product; then the SVD of B = Q^H M (l x n).  Returns
@@ -189,7 +214,7 @@ def _factor_sketch(M, l, power_iters, seed):
     E = M.clone()
     _ops.gemm(L.OP_N, L.OP_N, m, n, l, Q, l, B, n, E, n, alpha=-1.0, beta=1.0)
     residual = _ops.nrm2(E) ** 2
-    S, fB = _factor_full(B)
+    S, fB = _factor_full(B, core)
 
     def factors(k, kdev):
         UB, SV = fB(k, kdev)                                       # l x k, k x n
@@ -230,11 +255,12 @@ class RankStats:
         self.sketched = 0
         self.fallbacks = 0
         self.full = 0
+        self.declined = 0    # bonds whose neighbour was cut by the bond cap: no sketch tried
         self.rows_factored = 0   # sum over bonds of (rows of the Jacobi problem)^2 * row length
 
 
 def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None, oversample=16,
-                    power_iters=2, rank_stats=None, seed=1234):
+                    power_iters=2, rank_stats=None, seed=1234, core=None):
     """Truncating SVD branch of right_canonise (reverse, left_canonise,
     reverse; onedim_core.py:296-378) with normalise=False, in place on P.
 
@@ -249,6 +275,7 @@ def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None,
     N = len(P)
     norm_acc = 1.0
     s_prev = None
+    prev_disc = None   # discarded fraction of the previous bond's spectrum
     for i in range(N - 1, 0, -1):
         d, l, r = P[i].shape
         M = _ops.permute(P[i], (0, 2, 1)).reshape(d * r, l)  # rows (phys, right), cols left
@@ -259,12 +286,20 @@ def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None,
         if dw_tol is not None and rank_stats is not None or rank_model is not None:
             feats = RM.spectrum_features((i - 1) / max(N - 2, 1), kmax, chi or kmax, dw_tol or 1e-16,
                                          s_prev if s_prev is not None else np.ones(1))
-        if rank_model is not None and dw_tol is not None and s_prev is not None:
+        # a sketch can only be accepted where the tolerance, not the bond cap,
+        # decides the rank: the uncaptured weight must stay below dw_tol; where
+        # the neighbouring bond discarded more than 10 dw_tol (its cut set by
+        # chi) the full SVD runs without a sketch
+        cap_bound = prev_disc is not None and dw_tol is not None and prev_disc > 10.0 * dw_tol
+        if rank_model is not None and dw_tol is not None and s_prev is not None and cap_bound:
+            if rank_stats is not None:
+                rank_stats.declined += 1
+        elif rank_model is not None and dw_tol is not None and s_prev is not None:
             frac = float(rank_model.predict(feats)[0])
             lsk = min(kmax, int(math.ceil(frac * kmax)) + oversample)
             if lsk < 0.75 * kmax:
                 total = _ops.nrm2(M) ** 2
-                S, factors, residual = _factor_sketch(M, lsk, power_iters, seed + i)
+                S, factors, residual = _factor_sketch(M, lsk, power_iters, seed + i, core)
                 s_host = S.cpu().numpy().astype(np.float64)
                 if residual <= dw_tol * total:
                     used_sketch = True
@@ -280,7 +315,7 @@ def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None,
                 elif rank_stats is not None:
                     rank_stats.fallbacks += 1
         if not used_sketch:
-            S, factors = _factor_full(M)
+            S, factors = _factor_full(M, core)
             s_host = S.cpu().numpy().astype(np.float64)
             if dw_tol is None:
                 k = reference_rank(s_host, chi or 0, threshold)
@@ -300,6 +335,8 @@ def svd_right_sweep(P, chi, threshold, stats=None, dw_tol=None, rank_model=None,
             raise ValueError("zero state in the SVD sweep")
         if rank_stats is not None or rank_model is not None:
             s_prev = s_host
+            tot2 = float(np.sum(s_host ** 2))
+            prev_disc = disc / tot2 if tot2 > 0 else 0.0
         U, SV = factors(k, kd)
         P[i] = _ops.permute(U.reshape(d, r, k), (0, 2, 1))             # (phys, k, right)
         dp, lp, rp = P[i - 1].shape                                      # rp == l
@@ -318,7 +355,7 @@ _FOLD_LIMIT = {torch.complex64: 60.0, torch.float32: 60.0}  # |log| folded into 
 
 
 def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0, dw_tol=None,
-                   rank_model=None, rank_stats=None, oversample=16, power_iters=2):
+                   rank_model=None, rank_stats=None, oversample=16, power_iters=2, core=None):
     """One unit: contract_mps_mpo then svd_compress(chi, threshold,
     normalise=False).  ``sites`` / ``mpo`` are device tensors in (phys,
     left, right) / (physout, physin, left, right) layout, all of the compute
@@ -327,11 +364,14 @@ def apply_compress(sites, mpo, chi, threshold=1e-15, stats=None, log_norm_in=0.0
     state's norm in the first site, as svd_compress does; when that factor is
     outside the storage range (FP32: |log| > 60) it is left out of the sites
     and only reported in ``stats.log_norm``.  ``dw_tol``, ``rank_model``,
-    ``rank_stats``, ``oversample``, ``power_iters``: see svd_right_sweep."""
+    ``rank_stats``, ``oversample``, ``power_iters``: see svd_right_sweep.
+    ``core="fp64"`` (single-precision sites): every bond core's Jacobi is
+    finished in FP64 and the spectrum, the rank decision and U come from the
+    FP64 rows (the "mixed" precision, as ``apply_compress_native`` does)."""
     P = apply_mpo(sites, mpo)
     log_norm = qr_left_sweep(P) + log_norm_in
     norm_acc = svd_right_sweep(P, chi, threshold, stats, dw_tol=dw_tol, rank_model=rank_model,
-                               oversample=oversample, power_iters=power_iters, rank_stats=rank_stats)
+                               oversample=oversample, power_iters=power_iters, rank_stats=rank_stats, core=core)
     total = log_norm + (float(np.log(norm_acc)) if norm_acc > 0 else 0.0)
     # svd_right_sweep already folded norm_acc into P[0]
     lim = _FOLD_LIMIT.get(P[0].dtype, 600.0)
@@ -647,17 +687,48 @@ def apply_compress_batch(batch, mpo, chi, threshold=1e-15, streams=None, stats=N
     return out
 
 
-def inner_product(bra, ket, conj_bra=True):
+def _unit_site(x):
+    """(x / |x|_F, log |x|_F) for a device tensor whose squared norm may leave
+    the FP64 range (|x| > 1e154 or < 1e-154): it is first scaled by a power
+    of two, exactly."""
+    n = _ops.nrm2(x)
+    shift = 0.0
+    for _ in range(4):
+        if n > 0 and math.isfinite(n) and 1e-150 < n < 1e150:
+            break
+        if not math.isfinite(n):
+            step = -600
+        elif n == 0:
+            return x, 0.0
+        else:
+            step = 600 if n < 1e-150 else -600
+        x = _ops.scale(x, 2.0 ** step)
+        shift -= step * math.log(2.0)
+        n = _ops.nrm2(x)
+    if not (n > 0) or not math.isfinite(n):
+        return x, shift
+    return _ops.scale(x, 1.0 / n), shift + math.log(n)
+
+
+def inner_product(bra, ket, conj_bra=True, log_scale=False):
     """<bra|ket> of two (phys, left, right) site lists on the device, by the
     left-to-right environment sweep of ladder_contract (onedim_core.py:1587-1607).
-    Returns a Python complex."""
+    Returns a Python complex; with ``log_scale`` every site and the
+    environment after every site are rescaled to unit norm and (mantissa,
+    natural log of the scale) is returned, for states whose overlaps leave
+    the FP64 range."""
     dt = torch.promote_types(bra[0].dtype, ket[0].dtype)
     C = None
+    logs = 0.0
     for a, b in zip(bra, ket):
         a = _ops.cast(a, dt)
         b = _ops.cast(b, dt)
         if conj_bra:
             a = _ops.conj(a)
+        if log_scale:  # sites to unit norm too (one of them may hold the state's whole norm)
+            a, la_ = _unit_site(a)
+            b, lb_ = _unit_site(b)
+            logs += la_ + lb_
         d, la, ra = a.shape
         _, lb, rb = b.shape
         if C is None:
@@ -674,13 +745,22 @@ def inner_product(bra, ket, conj_bra=True):
         Xp = _ops.permute(X, (1, 0, 2)).reshape(ra, d * lb)
         _ops.gemm(L.OP_N, L.OP_N, ra, rb, d * lb, Xp, d * lb, b.reshape(d * lb, rb), rb, Cn, rb)
         C = Cn
+        if log_scale:
+            n = _ops.nrm2(C)
+            if n > 0:
+                C = _ops.scale(C, 1.0 / n)
+                logs += math.log(n)
     v = C.reshape(-1)[0].item()
-    return complex(v)
+    return (complex(v), logs) if log_scale else complex(v)
 
 
 def fidelity(a, b):
-    """|<a|b>|^2 / (<a|a><b|b>) on the device."""
-    ab = inner_product(a, b)
-    aa = inner_product(a, a).real
-    bb = inner_product(b, b).real
-    return abs(ab) ** 2 / (aa * bb)
+    """|<a|b>|^2 / (<a|a><b|b>) on the device, the overlaps carried as
+    logarithms (``inner_product(log_scale=True)``): the norms of long chains
+    leave the FP64 range."""
+    ab, lab = inner_product(a, b, log_scale=True)
+    aa, laa = inner_product(a, a, log_scale=True)
+    bb, lbb = inner_product(b, b, log_scale=True)
+    if ab == 0:
+        return 0.0
+    return math.exp(2.0 * (math.log(abs(ab)) + lab) - (math.log(aa.real) + laa) - (math.log(bb.real) + lbb))
