@@ -41,11 +41,12 @@ N_SITES, PHYS, MPO_D, CHI = 64, 2, 3, 256
 # lockstep and contend for the same resources at the same time
 STAGGER = 0.02
 METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, complex128)"
-# dram bytes (read + write) per call of the dominant native op at the
-# workload's bulk shape (the Jacobi kernel of tnc_svd_rows on the 512 x 512
-# complex64 triangular factor: 2.412 MB read + 0.470 MB written), from an
-# ncu capture of that kernel at that shape; absent = not captured.
-TRAFFIC_PER_CALL = {"tnc_svd_rows": 2.882e6}
+# dram bytes (read + write) per call of the native ops at the workload's bulk
+# shape, from ncu captures of their Jacobi kernels at that shape (the matrix
+# once in and once out; the working set stays in L2): the FP32 Jacobi on the
+# 512 x 512 complex64 factor 2.410 MB read + 0.488 MB written, the FP64 finish
+# on the 512 x 512 complex128 rows 5.191 MB + 0.435 MB; absent = not captured.
+TRAFFIC_PER_CALL = {"tnc_svd_rows": 2.898e6, "tnc_svd_rows_fp64_finish": 5.626e6}
 
 
 def parse():
