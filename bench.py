@@ -385,9 +385,34 @@ def run_ours(args):
     d2h = sum(a.nbytes for r in e2e_last for a in r)  # per step: B instances' results
     e2e_value = world * B * args.steps / e2e_el
 
+    # ---- the same sweep with the FP32 Jacobi alone on the bond cores (no FP64
+    # finish): the speed the FP64 core costs, and its accuracy
+    extra = {}
+    fp32_sites, fp32_stats = None, None
+    if args.precision == "mixed" and not args.no_plain:
+        last32, stats32 = [None] * B, [None] * B
+        kw32 = dict(precision_core=None, out=last32, stats=stats32)
+        run_steps(1, **kw32)
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(st)
+        run_steps(1, **kw32)
+        e1.record(st)
+        barrier()
+        t32 = e0.elapsed_time(e1) / 1e3
+        if world > 1:
+            t = torch.tensor([t32], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t32 = float(t.item())
+        extra["fp32_core"] = {"value": world * B / t32, "unit": "sweeps/s", "steps": 1, "warmup": 1,
+                              "path": "the same native sweep with the FP32 Jacobi alone on every bond core"}
+        fp32_sites = [a.cpu().numpy() for a in last32[0]]
+        fp32_stats = stats32[0]
+
     # ---- the plain FP64 method of this project: the same native sweep and
     # work queue in complex128 end to end (QR, Jacobi, products, decision)
-    extra = {}
     fp64_sites, fp64_stats = None, None
     if not args.no_plain:
         dt64 = torch.complex128
@@ -482,6 +507,10 @@ def run_ours(args):
                                                  st0.discarded, ref, ref_df)}
         errs[args.precision]["bond_dims_match"] = [1] + list(st0.bonds) + [1] == \
             [1] + [a.shape[2] for a in ref[:-1]] + [1]
+        if fp32_sites is not None:
+            errs["fp32_core"] = errors_vs_oracle(fp32_sites, None if fp32_stats.norm_folded else fp32_stats.log_norm,
+                                                 fp32_stats.discarded, ref, ref_df)
+            errs["fp32_core"]["bond_dims_match"] = list(fp32_stats.bonds) == [a.shape[2] for a in ref[:-1]]
         if fp64_sites is not None:
             errs["fp64"] = errors_vs_oracle(fp64_sites, None if fp64_stats.norm_folded else fp64_stats.log_norm,
                                             fp64_stats.discarded, ref, ref_df)
