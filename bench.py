@@ -47,6 +47,10 @@ METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, compl
 # 512 x 512 complex64 factor 2.410 MB read + 0.488 MB written, the FP64 finish
 # on the 512 x 512 complex128 rows 5.191 MB + 0.435 MB; absent = not captured.
 TRAFFIC_PER_CALL = {"tnc_svd_rows": 2.898e6, "tnc_svd_rows_fp64_finish": 5.626e6}
+# the bond-core finish of the mixed precision, by its arithmetic
+FINISH_OP = {"df": "tnc_svd_rows_df", "fp64": "tnc_svd_rows_fp64_finish"}
+# FP32 pipe: 152 SMs x 128 lanes x 2.07 GHz operations/s (x 2 for FMA flops)
+FP32_OPS_T = 152 * 128 * 2.07e9 / 1e12
 
 
 def parse():
@@ -60,6 +64,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batch", type=int, default=12, help="independent instances per GPU")
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
+    p.add_argument("--core", default="df", choices=["df", "fp64"],
+                   help="the mixed precision's bond-core finish: double-float or FP64 arithmetic")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 engine arm")
     p.add_argument("--fp64-steps", type=int, default=1, help="timed steps of the plain FP64 engine arm")
     p.add_argument("--workload", default="tfim", choices=["tfim", "uneven", "learned"],
@@ -288,7 +294,8 @@ def run_ours(args):
 
     N, chi, B = args.nsites, args.chi, args.batch
     warm = max(args.warmup, 3)
-    core = "fp64" if args.precision == "mixed" else None
+    core = args.core if args.precision == "mixed" else None
+    E.MIXED_CORE = args.core
     # instance b of rank r uses seed (r * B + b); every instance is a full
     # workload; the caller's data is complex128 on the host
     host_batch = [W.random_mps_arrays(rank * B + b, N, PHYS, chi, np.complex128, normalise=True)
@@ -309,7 +316,7 @@ def run_ours(args):
     dev_mpo = E.to_sites(host_mpo, dt)
     last = [None] * B
     last_stats = [None] * B
-    OPS = ("tnc_qr", "tnc_qr_r", "tnc_svd_rows", "tnc_svd_rows_fp64_finish")
+    OPS = ("tnc_qr", "tnc_qr_r", "tnc_svd_rows", FINISH_OP[args.core])
 
     def sweep_job(b, prof=None, precision_core=core, batch=dev_batch, mpo=dev_mpo, out=last, stats=last_stats):
         def job():
@@ -453,12 +460,21 @@ def run_ours(args):
         peak, peak_src = 1900.0, "fallback"
     achieved = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
     fp64_op = name.endswith("fp64_finish")
-    pipe = ("FP64", 1.25) if fp64_op else ("FP32", 80.5)
-    fp_note = ("CUDA-core arithmetic (Jacobi rotations, Householder); frac is against the measured bf16 tensor "
-               "peak, frac_of_pipe_nominal against GB300's nominal %s CUDA-core rate (%s TFLOP/s%s); flops are "
-               "%s" % (pipe[0], pipe[1], "" if fp64_op else ": 152 SMs x 128 FMA x 2 x 2.07 GHz",
-                       "the FP64 Jacobi's executed flops (14 n^2 L per rotating sweep, 4 n^2 L for the checking "
-                       "one)" if fp64_op else "the op's fixed algorithmic count"))
+    df_op = name == FINISH_OP["df"]
+    if df_op:
+        pipe = ("FP32 (double-float operations)", round(FP32_OPS_T, 1))
+        fp_note = ("CUDA-core arithmetic; achieved counts the FP32 operations the double-float Jacobi executed "
+                   "(44 n^2 L per rotating sweep and 24 n^2 L for the checking one: 12 per Dot2 step, 7 per "
+                   "compensated update), frac is against the measured bf16 tensor peak, frac_of_pipe_nominal "
+                   "against the FP32 pipe's operation rate (152 SMs x 128 lanes x 2.07 GHz = %.1f T ops/s)"
+                   % FP32_OPS_T)
+    else:
+        pipe = ("FP64", 1.25) if fp64_op else ("FP32", 80.5)
+        fp_note = ("CUDA-core arithmetic (Jacobi rotations, Householder); frac is against the measured bf16 "
+                   "tensor peak, frac_of_pipe_nominal against GB300's nominal %s CUDA-core rate (%s TFLOP/s%s); "
+                   "flops are %s" % (pipe[0], pipe[1], "" if fp64_op else ": 152 SMs x 128 FMA x 2 x 2.07 GHz",
+                                     "the FP64 Jacobi's executed flops (14 n^2 L per rotating sweep, 4 n^2 L for "
+                                     "the checking one)" if fp64_op else "the op's fixed algorithmic count"))
     roofline = {"bound": "tensor", "kernel": name, "launches": ncalls, "achieved": achieved,
                 "measured": "CUDA events around every %s call, recorded by the native sweep on its instance's "
                             "stream in one profiled step of the same workload after the timed region (%d streams "
@@ -468,9 +484,11 @@ def run_ours(args):
                 "frac_of_pipe_nominal": achieved / pipe[1], "note": fp_note}
     tot_ms = sum(x[1] for x in timed.values())
     share = {k: round(v[1] / tot_ms, 4) for k, v in timed.items() if tot_ms > 0}
-    dtype_name = {"mixed": "c64+f64core", "fp32": "c64", "fp64": "c128"}[args.precision]
-    path = {"mixed": "engine (mixed: complex64 sites and FP32 products and QR, FP32 Jacobi finished by an FP64 "
-                     "Jacobi on every bond core, truncation decided on FP64 singular values)",
+    dtype_name = {"mixed": "c64+%score" % {"df": "df", "fp64": "f64"}[args.core], "fp32": "c64",
+                  "fp64": "c128"}[args.precision]
+    path = {"mixed": "engine (mixed: complex64 sites and FP32 products and QR, FP32 Jacobi finished by a %s "
+                     "Jacobi on every bond core, truncation decided on its singular values)"
+                     % {"df": "double-float (FP32-pipe, ~48-bit)", "fp64": "FP64"}[args.core],
             "fp32": "engine (fp32)", "fp64": "engine (fp64)"}[args.precision]
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": warm, "ms_per_step": elapsed / args.steps * 1e3,
@@ -682,6 +700,7 @@ def run_learned(args):
     from tncontract_gb300 import learned as LR
     from tncontract_gb300 import workloads as W
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    E.MIXED_CORE = args.core
     N, chi, tol = args.nsites, args.chi, 1e-8
     t0 = time.perf_counter()
     model, hist, ntrain = LR.train_rank_model(tol)
@@ -702,11 +721,13 @@ def run_learned(args):
                       "discarded weight <= 1e-8)" % (N, chi),
             "value": 1.0 / t_learn, "unit": "sweeps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": t_learn * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64core", "data": "synthetic (seeded random MPS, XXZ MPO)",
+            "dtype": "f32+%score" % {"df": "df", "fp64": "f64"}[E.MIXED_CORE],
+            "data": "synthetic (seeded random MPS, XXZ MPO)",
             "config": {"workload": "config5_learned_rank", "nsites": N, "phys_dim": 2, "mpo_bond": 5, "chi": chi,
                        "dw_tol": tol, "oversample": 16, "power_iters": 2,
                        "timing": "one sweep each, host wall clock around a synchronised sweep"},
-            "precision": "mixed (float32 sites and products, FP64 Jacobi finish of every bond core)",
+            "precision": "mixed (float32 sites and products, %s Jacobi finish of every bond core)"
+                         % {"df": "double-float", "fp64": "FP64"}[E.MIXED_CORE],
             "plain_sweeps_per_s": 1.0 / t_plain, "fp64_sweeps_per_s": 1.0 / t_ref,
             "fp32_core_sweeps_per_s": 1.0 / t_f32, "fidelity_error_fp32_core_vs_fp64": fid(f32, ref),
             "speedup_learned_vs_plain": t_plain / t_learn,

@@ -281,6 +281,36 @@ int tnc_svd_rows(int dtype, int64_t m, int64_t n, const void *A, void *W,
                  int block_rows, void *work, size_t work_bytes, int *info,
                  void *stream);
 
+/* tnc_svd_rows where only the first nkeep rows of W must come out orthogonal
+ * to every row: pairs of rows that both lie beyond nkeep (in whole
+ * half-blocks) take no rotation, so those rows are orthogonal to the kept
+ * ones but not among themselves, and their norms are their singular values
+ * only to the accuracy of W's start.  For a start whose rows are already
+ * nearly orthogonal and sorted by norm (the FP64 finish of a truncating
+ * bond: the rows beyond the retained rank are discarded), this saves the
+ * discarded-discarded rotations.  nkeep >= min(m, n) is tnc_svd_rows. */
+int tnc_svd_rows_keep(int dtype, int64_t m, int64_t n, const void *A, void *W,
+                      void *S, int64_t *order, int max_sweeps, double tol,
+                      int block_rows, int64_t nkeep, void *work,
+                      size_t work_bytes, int *info, void *stream);
+
+/* The extended-precision finish of single-precision rows, in double-float
+ * arithmetic on the FP32 pipe (a real number as an unevaluated pair of
+ * floats, about 48 significant bits; error-free TwoSum / TwoProd and Dot2
+ * inner products): GB300 issues FP32 fused multiply-adds about 70 times as
+ * fast as FP64 ones.  A: m x n rows (m <= n) of dtype TNC_F32 or TNC_C64,
+ * scaled by a power of two to unit Frobenius norm inside; W (m x n) receives
+ * the orthogonalised rows as FP64 / complex128 elements, S (FP64) and order
+ * as tnc_svd_rows for the FP64 type, and the rows are orthogonal to tol
+ * relative (<= 0: 1e-7).  Rows beyond nkeep as in tnc_svd_rows_keep.  Rows
+ * up to 800 complex / 1600 real elements.  Workspace:
+ * tnc_svd_rows_workspace_size of the FP64 type.  Replaces, in the sweep,
+ * the FP64 finish (tnc_cast to the FP64 type + tnc_svd_rows_keep). */
+int tnc_svd_rows_df(int dtype, int64_t m, int64_t n, const void *A, void *W,
+                    void *S, int64_t *order, int max_sweeps, double tol,
+                    int block_rows, int64_t nkeep, void *work,
+                    size_t work_bytes, int *info, void *stream);
+
 /* dst <- rows order[0:k] of src (row length L), k read from device memory
  * (capped by kmax): mode 0 copies rows (dst k x L); mode 1 writes
  * dst[c][i] = conj(src[order[i]][c]) / S[i] (dst L x k, leading dim k).
@@ -309,7 +339,8 @@ int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
  * storage-precision Jacobi, and takes the singular values, the truncation
  * decision and U from the FP64 rows (the storage-precision stage then runs
  * to 3e-6 and at most 14 sweeps, a stall above that handing over to the FP64
- * stage).  core_tol: the FP64 stage's tolerance (<= 0: 1e-7, pairs of rows
+ * stage); TNC_CORE_DF (2) is the same with the finish in double-float
+ * arithmetic (tnc_svd_rows_df) instead of FP64.  core_tol: the FP64 stage's tolerance (<= 0: 1e-7, pairs of rows
  * orthogonal to 1e-7 relative, the rounding level of U's single-precision
  * storage; the singular values' error from it is second order).  The
  * singular values inherit the storage-precision stage's rounding (FP32-class
@@ -325,8 +356,10 @@ int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
  * [3o+1] += calls, [3o+2] += the op's fixed algorithmic flops (for op 3 the
  * flops the FP64 Jacobi executed: 14 n^2 L per rotating sweep and 4 n^2 L for
  * the last, checking one, n rows of length L, complex; a third of that
- * real).  Returns TNC_ERR_ARG for a zero state. */
-enum { TNC_CORE_STORAGE = 0, TNC_CORE_FP64 = 1 };
+ * real; for TNC_CORE_DF the FP32 operations of the double-float Jacobi:
+ * 44 n^2 L per rotating sweep and 24 n^2 L for the checking one, complex;
+ * 15 and 6 real).  Returns TNC_ERR_ARG for a zero state. */
+enum { TNC_CORE_STORAGE = 0, TNC_CORE_FP64 = 1, TNC_CORE_DF = 2 };
 int tnc_sweep_workspace_size(int dtype, int n_sites, int64_t d,
                              const int64_t *mps_bonds, const int64_t *mpo_bonds,
                              int core, size_t *bytes);

@@ -16,7 +16,7 @@ from . import _build
 F32, F64, C64, C128 = 0, 1, 2, 3
 OK, ERR_ARG, ERR_NOT_CONVERGED, ERR_NONFINITE, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_TOO_LARGE = range(8)
 OP_N, OP_T, OP_C, OP_R = 0, 1, 2, 3
-CORE_STORAGE, CORE_FP64 = 0, 1
+CORE_STORAGE, CORE_FP64, CORE_DF = 0, 1, 2
 
 _vp = C.c_void_p
 _i64 = C.c_int64
@@ -73,6 +73,8 @@ SIGNATURES = {
     "tnc_svd_noalloc": [_int, _i64, _i64, _vp, _i64, _vp, _vp, _vp, _int, _dbl, _vp, _vp],
     "tnc_svd_rows_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_svd_rows": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _vp, C.c_size_t, _vp, _vp],
+    "tnc_svd_rows_keep": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _i64, _vp, C.c_size_t, _vp, _vp],
+    "tnc_svd_rows_df": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _i64, _vp, C.c_size_t, _vp, _vp],
     "tnc_gather_rows": [_int, _vp, _i64, _vp, _vp, _i64, _vp, _int, _vp, _vp],
     "tnc_gemm_tc_workspace_size": [_int, _i64, _i64, _i64, _i64, _psz],
     "tnc_gemm_tc": [_int, _int, _int, _i64, _i64, _i64, _pdbl, _vp, _i64, _i64, _vp, _i64, _i64, _pdbl,

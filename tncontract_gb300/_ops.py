@@ -738,6 +738,26 @@ def svd_rows(M, max_sweeps=0, tol=0.0, block_rows=None):
     return W, S, order, info
 
 
+def svd_rows_df(M, max_sweeps=0, tol=0.0, block_rows=0, nkeep=None):
+    """Double-float Jacobi of the rows of a wide single-precision M
+    (``tnc_svd_rows_df``): returns (W, S, order, info) as ``svd_rows`` of M
+    widened to FP64 (W complex128 / float64, S float64); ``nkeep``: only the
+    first nkeep rows need be orthogonal to every row (None: all)."""
+    M = M.contiguous()
+    m, n = M.shape
+    wide = torch.complex128 if is_complex(M.dtype) else torch.float64
+    W = empty((m, n), wide)
+    S = empty((m,), torch.float64)
+    order = torch.empty(m, dtype=torch.int64, device=device())
+    info = torch.empty(4, dtype=torch.int32, device=device())
+    sz = C.c_size_t()
+    _call("tnc_svd_rows_workspace_size", code(wide), m, n, C.byref(sz))
+    ws = workspace(sz.value)
+    _call("tnc_svd_rows_df", code(M.dtype), m, n, _p(M), _p(W), _p(S), _p(order), int(max_sweeps), float(tol),
+          int(block_rows), m if nkeep is None else int(nkeep), _p(ws), sz.value, _p(info), _stream())
+    return W, S, order, info
+
+
 def fill_gaussian(shape, dtype, seed):
     out = empty(shape, dtype)
     if out.numel():

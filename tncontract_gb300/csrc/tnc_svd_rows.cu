@@ -25,9 +25,11 @@
 // and each rotation streams its rows through registers and shared memory
 // instead of L2.  One cooperative launch runs all sweeps; every wait is
 // bounded (tnc_persist.cuh).
+#include "tnc_df.cuh"
 #include "tnc_persist.cuh"
 
 #include <atomic>
+#include <type_traits>
 
 namespace tnc {
 
@@ -175,6 +177,180 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
   for (int64_t e = threadIdx.x; e < total; e += blockDim.x) stcg(W + row0 * L + e, s[e]);
 }
 
+// ------------------------------------------------------------ DF rows
+// The extended-precision finish (tnc_svd_rows_df) runs the same kernel on
+// double-float rows (tnc_df.cuh); these overloads are its rotation and norm.
+
+// Jacobi rotation of two DF rows from their carried squared norms a, b and
+// g = <x, y>, same formula as make_rot.  A small angle (|t| < 2^-12, the
+// finish's usual case: rows already orthogonal to FP32 level) is computed in
+// FP32 and applied as x + ((c - 1) x - s e y): the FP32 rounding then falls on
+// the small correction only, 2^-24 |t| relative to the row, and the
+// transformation stays orthogonal to 4 eps t^2.  A larger angle (two rows
+// of nearly equal norm) takes the FP64 formula on the DF inputs and a full DF
+// product.
+struct RotDF {
+  bool apply, big;
+  float cm1, ser, sei;  // small angle: c - 1 and s e (e = g / |g|)
+  dfr c, sr, si;        // large angle: c and s e
+  dfr a, b;             // the rows' new squared norms
+};
+
+__device__ __forceinline__ RotDF make_rot_df(dfr a, dfr b, dfr gre, dfr gim, float rtol, float noise2, bool cplx) {
+  RotDF r;
+  r.apply = false;
+  r.big = false;
+  const float gabs = cplx ? hypotf(gre.h, gim.h) : fabsf(gre.h);
+  // rows at the rounding-noise floor count as converged (as make_rot)
+  if (!(a.h > noise2 && b.h > noise2 && gabs > rtol * sqrtf(a.h) * sqrtf(b.h))) return r;
+  float ds, de;
+  two_sum(b.h, -a.h, ds, de);
+  de = __fadd_rn(de, __fsub_rn(b.l, a.l));
+  const float tau = __fadd_rn(ds, de) / (2.f * gabs);
+  if (fabsf(tau) >= 4096.f) {
+    const float t = fabsf(tau) > 1e7f ? 0.5f / tau
+                                      : (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
+    if (t == 0.f) return r;  // below FP32 range: nothing to rotate
+    const float q = sqrtf(fmaf(t, t, 1.f));
+    const float s = t / q, inv = 1.f / gabs;
+    r.apply = true;
+    r.cm1 = -(t * t) / (q * (1.f + q));
+    r.ser = s * (gre.h * inv);
+    r.sei = cplx ? s * (gim.h * inv) : 0.f;
+    const float th = t * gabs;
+    r.a = df_add(a, dfr(-th, 0.f));
+    r.b = df_add(b, dfr(th, 0.f));
+    return r;
+  }
+  const double ad = to_double(a), bd = to_double(b);
+  const double gr = to_double(gre), gi = cplx ? to_double(gim) : 0.0;
+  const double h = cplx ? hypot(gr, gi) : fabs(gr);
+  const double taud = (bd - ad) / (2.0 * h);
+  const double t = (taud >= 0 ? 1.0 : -1.0) / (fabs(taud) + sqrt(1.0 + taud * taud));
+  const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+  r.apply = true;
+  r.big = true;
+  r.c = dfr(c);
+  r.sr = dfr(s * (gr / h));
+  r.si = dfr(cplx ? s * (gi / h) : 0.0);
+  const double th = t * h;
+  r.a = dfr(ad - th);
+  r.b = dfr(bd + th);
+  return r;
+}
+
+__device__ __forceinline__ dfr df_neg(dfr v) { return dfr(-v.h, -v.l); }
+// c u + p v + q w in DF
+__device__ __forceinline__ dfr df_dot3(dfr c, dfr u, dfr p, dfr v, dfr q, dfr w) {
+  return df_add(df_add(df_mul(c, u), df_mul(p, v)), df_mul(q, w));
+}
+
+// complex DF rows x, y in shared memory, one warp; squared norms carried
+__device__ __forceinline__ bool rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b) {
+  const int lane = threadIdx.x & 31;
+  // g = sum x conj(y): Re = xr yr + xi yi, Im = xi yr - xr yi, four Dot2 chains
+  float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f, s3 = 0.f, c3 = 0.f;
+  for (int64_t k = lane; k < L; k += 32) {
+    const dfc xv = x[k], yv = y[k];
+    dot2_acc(s0, c0, xv.re.h, xv.re.l, yv.re.h, yv.re.l);
+    dot2_acc(s1, c1, xv.im.h, xv.im.l, yv.im.h, yv.im.l);
+    dot2_acc(s2, c2, xv.im.h, xv.im.l, yv.re.h, yv.re.l);
+    dot2_acc(s3, c3, -xv.re.h, -xv.re.l, yv.im.h, yv.im.l);
+  }
+  const dfr gre = warp_sum_df(df_add(df_norm(s0, c0), df_norm(s1, c1)));
+  const dfr gim = warp_sum_df(df_add(df_norm(s2, c2), df_norm(s3, c3)));
+  const RotDF r = make_rot_df(*a, *b, gre, gim, rtol.h, noise2.h, true);
+  if (!r.apply) return false;
+  if (!r.big) {
+    // x += (c-1) x - se y, y += conj(se) x + (c-1) y, from the hi parts
+    const float cm1 = r.cm1, ser = r.ser, sei = r.sei;
+    for (int64_t k = lane; k < L; k += 32) {
+      dfc xv = x[k], yv = y[k];
+      const float xr = xv.re.h, xi = xv.im.h, yr = yv.re.h, yi = yv.im.h;
+      const float syr = fmaf(ser, yr, -sei * yi), syi = fmaf(ser, yi, sei * yr);
+      const float sxr = fmaf(ser, xr, sei * xi), sxi = fmaf(ser, xi, -sei * xr);
+      df_acc(xv.re, fmaf(cm1, xr, -syr));
+      df_acc(xv.im, fmaf(cm1, xi, -syi));
+      df_acc(yv.re, fmaf(cm1, yr, sxr));
+      df_acc(yv.im, fmaf(cm1, yi, sxi));
+      x[k] = xv;
+      y[k] = yv;
+    }
+  } else {
+    // x' = c x - se y, y' = conj(se) x + c y in DF
+    const dfr c = r.c, sr = r.sr, si = r.si, nsr = df_neg(r.sr), nsi = df_neg(r.si);
+    for (int64_t k = lane; k < L; k += 32) {
+      const dfc xv = x[k], yv = y[k];
+      dfc nx, ny;
+      nx.re = df_dot3(c, xv.re, nsr, yv.re, si, yv.im);
+      nx.im = df_dot3(c, xv.im, nsr, yv.im, nsi, yv.re);
+      ny.re = df_dot3(c, yv.re, sr, xv.re, si, xv.im);
+      ny.im = df_dot3(c, yv.im, sr, xv.im, nsi, xv.re);
+      x[k] = nx;
+      y[k] = ny;
+    }
+  }
+  __syncwarp();
+  if (lane == 0) { *a = r.a; *b = r.b; }
+  __syncwarp();
+  return true;
+}
+
+// real DF rows
+__device__ __forceinline__ bool rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b) {
+  const int lane = threadIdx.x & 31;
+  float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+  int64_t k = lane;
+  for (; k + 32 < L; k += 64) {
+    const dfr x0 = x[k], y0 = y[k], x1 = x[k + 32], y1 = y[k + 32];
+    dot2_acc(s0, c0, x0.h, x0.l, y0.h, y0.l);
+    dot2_acc(s1, c1, x1.h, x1.l, y1.h, y1.l);
+  }
+  if (k < L) dot2_acc(s0, c0, x[k].h, x[k].l, y[k].h, y[k].l);
+  const dfr g = warp_sum_df(df_add(df_norm(s0, c0), df_norm(s1, c1)));
+  const RotDF r = make_rot_df(*a, *b, g, dfr(0.f, 0.f), rtol.h, noise2.h, false);
+  if (!r.apply) return false;
+  if (!r.big) {
+    const float cm1 = r.cm1, se = r.ser;
+    for (int64_t kk = lane; kk < L; kk += 32) {
+      dfr xv = x[kk], yv = y[kk];
+      const float xh = xv.h, yh = yv.h;
+      df_acc(xv, fmaf(cm1, xh, -se * yh));
+      df_acc(yv, fmaf(cm1, yh, se * xh));
+      x[kk] = xv;
+      y[kk] = yv;
+    }
+  } else {
+    const dfr c = r.c, s = r.sr, ns = df_neg(r.sr), zero(0.f, 0.f);
+    for (int64_t kk = lane; kk < L; kk += 32) {
+      const dfr xv = x[kk], yv = y[kk];
+      x[kk] = df_dot3(c, xv, ns, yv, zero, zero);
+      y[kk] = df_dot3(c, yv, s, xv, zero, zero);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) { *a = r.a; *b = r.b; }
+  __syncwarp();
+  return true;
+}
+
+__device__ __forceinline__ dfr warp_row_norm2(const dfc* x, int64_t L) {
+  const int lane = threadIdx.x & 31;
+  float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+  for (int64_t k = lane; k < L; k += 32) {
+    const dfc v = x[k];
+    dot2_acc(s0, c0, v.re.h, v.re.l, v.re.h, v.re.l);
+    dot2_acc(s1, c1, v.im.h, v.im.l, v.im.h, v.im.l);
+  }
+  return warp_sum_df(df_add(df_norm(s0, c0), df_norm(s1, c1)));
+}
+__device__ __forceinline__ dfr warp_row_norm2(const dfr* x, int64_t L) {
+  const int lane = threadIdx.x & 31;
+  float s0 = 0.f, c0 = 0.f;
+  for (int64_t k = lane; k < L; k += 32) dot2_acc(s0, c0, x[k].h, x[k].l, x[k].h, x[k].l);
+  return warp_sum_df(df_norm(s0, c0));
+}
+
 // Step counters of the half-blocks: ver[b] = steps completed on half-block b
 // (phase 0 and the rounds, counted across sweeps).  The CTA that finished a
 // step on P and Q publishes after its rows are stored; the CTA that takes them
@@ -222,16 +398,20 @@ __device__ __forceinline__ bool wait_steps(const unsigned* ver, int64_t P, int64
 // clock per SM on GB300, measured), not by shared-memory traffic, and the other
 // half of the register file stays free for an FP32 kernel of another instance
 // on the same SM (a register-resident FP64 row took all 255 registers a
-// thread, so nothing else could share the SM).
+// thread, so nothing else could share the SM).  Double-float rows fill the
+// shared memory of an SM with one CTA (2 x 8 rows of 512 16-byte elements)
+// and keep the registers of their Dot2 chains.
 template <typename T, int MAXE, int MAXT, bool PREG>
 constexpr int jacobi_min_blocks() {
+  if (std::is_same<T, dfc>::value || std::is_same<T, dfr>::value) return 1;
   return (!PREG || (MAXT == 256 && MAXE <= 16 && sizeof(typename traits<T>::real) == 4)) ? 2 : 1;
 }
 
 template <typename T, int MAXE, int MAXT, bool PREG>
 __global__ void __launch_bounds__(MAXT, jacobi_min_blocks<T, MAXE, MAXT, PREG>())
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
-                    typename traits<T>::real* Dn, unsigned* counters, unsigned* ver, SyncWords* sw, int* info) {
+                    typename traits<T>::real* Dn, unsigned* counters, unsigned* ver, SyncWords* sw, int* info,
+                    int64_t nkeep) {
   typedef typename traits<T>::real R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sB = reinterpret_cast<T*>(smem_raw);
@@ -241,6 +421,9 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
   const int64_t nb = (nr + h - 1) / h;
   const int64_t nbp = nb + (nb & 1);
   const int64_t ntask = nbp / 2;
+  // half-blocks holding the first nkeep rows; pairs of two later half-blocks
+  // take no rotation (their rows need only be orthogonal to the kept ones)
+  const int64_t kb = (nkeep + h - 1) / h;
   const R rtol = (R)tol;
   const R noise2 = noise_floor2<T>(frob2);
   int sweep = 0;
@@ -266,7 +449,7 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
       }
       __syncthreads();
       const int hp = h + (h & 1);
-      for (int rr = 0; rr < hp - 1; ++rr) {
+      for (int rr = 0; hb < kb && rr < hp - 1; ++rr) {
         if (warp < hp / 2) {
           int64_t p, q;
           circle_pair(hp, rr, warp, p, q);
@@ -293,6 +476,10 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
           continue;
         }
         if (!wait_steps(ver, P, Q, g, sw)) return;
+        if (P >= kb && Q >= kb) {  // two discarded half-blocks: pass them on
+          publish_steps(ver, P, Q, g + 1u);
+          continue;
+        }
         const int64_t q0 = Q * h;
         const int cntB = (int)((nr - q0) < h ? (nr - q0) : h);
         if constexpr (PREG) {
@@ -475,7 +662,8 @@ static int ensure_smem_attr() {
 
 template <typename T, int MAXE, int MAXT, bool PREG = true>
 static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, const double* frob2,
-                        typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info, cudaStream_t st) {
+                        typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info, int64_t nkeep,
+                        cudaStream_t st) {
   const size_t smem = (size_t)(PREG ? 1 : 2) * h * L * sizeof(T);
   const void* fn = (const void*)jacobi_block_kernel<T, MAXE, MAXT, PREG>;
   if (smem > kMaxHalfBlockBytes || 32 * h > MAXT) return TNC_ERR_ARG;
@@ -494,15 +682,16 @@ static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, 
   int64_t nr_ = nr, L_ = L;
   int h_ = h, ms_ = ms;
   double tol_ = tol;
-  void* args[] = {(void*)&W, (void*)&nr_, (void*)&L_, (void*)&h_, (void*)&ms_, (void*)&tol_,
-                  (void*)&frob2, (void*)&Dn, (void*)&counters, (void*)&ver, (void*)&sw, (void*)&info};
+  int64_t nkeep_ = nkeep;
+  void* args[] = {(void*)&W,  (void*)&nr_, (void*)&L_,       (void*)&h_,  (void*)&ms_, (void*)&tol_,   (void*)&frob2,
+                  (void*)&Dn, (void*)&counters, (void*)&ver, (void*)&sw, (void*)&info, (void*)&nkeep_};
   if (cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, st) != cudaSuccess) return TNC_ERR_CUDA;
   return TNC_OK;
 }
 
 template <typename T>
 static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits<T>::real* S, int64_t* order,
-                         int max_sweeps, double tol, int block_rows, void* work, size_t wb, int* info,
+                         int max_sweeps, double tol, int block_rows, int64_t nkeep, void* work, size_t wb, int* info,
                          cudaStream_t st) {
   typedef typename traits<T>::real R;
   if (m <= 0 || n <= 0 || !A || !W || !S || !order || !work || !info) return TNC_ERR_ARG;
@@ -510,6 +699,7 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
   const int64_t nr = tall ? n : m, L = tall ? m : n;
   RowsLayout Ly = rows_layout(nr, sizeof(R));
   if (wb < Ly.total) return TNC_ERR_WORKSPACE;
+  if (nkeep > nr) nkeep = nr;  // every row kept (the kernel rounds nkeep up to half-blocks)
   if (max_sweeps <= 0) max_sweeps = 40;
   if (max_sweeps > kRowsMaxSweeps) max_sweeps = kRowsMaxSweeps;
   if (tol <= 0) tol = sqrt((double)(L > 8 ? L : 8)) * traits<T>::eps * (sizeof(R) == 4 ? 4.0 : 1.0);
@@ -552,20 +742,20 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
       // FP64 rows: both half-blocks in shared memory (2 h L elements)
       if (h > 8) h = 8;
       while (h > 2 && (size_t)2 * h * L * sizeof(T) > kMaxHalfBlockBytes) h >>= 1;
-      rc = launch_block<T, 1, 256, false>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+      rc = launch_block<T, 1, 256, false>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
     } else if (h == 16) {
       if constexpr (sizeof(T) <= 8) {
-        if (L <= 256) rc = launch_block<T, 8, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
-        else rc = launch_block<T, 16, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+        if (L <= 256) rc = launch_block<T, 8, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
+        else rc = launch_block<T, 16, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
       } else {
         return TNC_ERR_ARG;
       }
     } else if (L <= 256) {
-      rc = launch_block<T, 8, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+      rc = launch_block<T, 8, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
     } else if (L <= 512) {
-      rc = launch_block<T, 16, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+      rc = launch_block<T, 16, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
     } else if (L <= 1024 && !big) {
-      if constexpr (sizeof(T) < 16) rc = launch_block<T, 32, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, st);
+      if constexpr (sizeof(T) < 16) rc = launch_block<T, 32, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
       else return TNC_ERR_ARG;
     } else {
       return TNC_ERR_ARG;  // rows too long for the register-resident half block
@@ -588,6 +778,89 @@ static int gather_impl(const T* src, int64_t L, const int64_t* order, const int6
   return launch_status();
 }
 
+// ------------------------------------------------------------ DF finish
+// Exponent k with |A|_F about 2^k: the DF rows are A 2^-k, inside FP32's range.
+__device__ __forceinline__ int df_scale_exp(const double* f2) {
+  const double f = f2[0];
+  return (f > 0.0 && isfinite(f)) ? ilogb(sqrt(f)) : 0;
+}
+__device__ __forceinline__ dfr df_widen(float v, int k) { return dfr(ldexpf(v, -k), 0.f); }
+__device__ __forceinline__ dfc df_widen(c64 v, int k) {
+  dfc r;
+  r.re = dfr(ldexpf(v.re, -k), 0.f);
+  r.im = dfr(ldexpf(v.im, -k), 0.f);
+  return r;
+}
+__device__ __forceinline__ double df_narrow(dfr v, int k) { return ldexp(to_double(v), k); }
+__device__ __forceinline__ c128 df_narrow(dfc v, int k) { return c128(ldexp(to_double(v.re), k), ldexp(to_double(v.im), k)); }
+
+// W = A 2^-k as DF; frob2[1] = frob2[0] 2^-2k (the scaled rows' squared norm)
+template <typename Tin, typename Tdf>
+__global__ void df_widen_kernel(int64_t n, const Tin* A, Tdf* W, double* frob2) {
+  const int k = df_scale_exp(frob2);
+  if (blockIdx.x == 0 && threadIdx.x == 0) frob2[1] = ldexp(frob2[0], -2 * k);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    W[i] = df_widen(A[i], k);
+}
+// in place: the DF element i becomes the FP64 element i (same size) times 2^k
+template <typename Tdf, typename Tout>
+__global__ void df_narrow_kernel(int64_t n, Tdf* W, const double* frob2) {
+  static_assert(sizeof(Tdf) == sizeof(Tout), "in-place narrowing keeps the element size");
+  const int k = df_scale_exp(frob2);
+  Tout* out = reinterpret_cast<Tout*>(W);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const Tdf v = W[i];
+    out[i] = df_narrow(v, k);
+  }
+}
+
+// The finish of single-precision rows in double-float: A (m x n, m <= n,
+// FP32 or complex64) -> W (m x n, FP64 / complex128 elements), S (FP64), order.
+template <typename Tin, typename Tdf, typename Tout>
+static int svd_rows_df_impl(int64_t m, int64_t n, const Tin* A, void* Wv, double* S, int64_t* order, int max_sweeps,
+                            double tol, int block_rows, int64_t nkeep, void* work, size_t wb, int* info,
+                            cudaStream_t st) {
+  if (m <= 0 || n <= 0 || m > n || !A || !Wv || !S || !order || !work || !info || nkeep < 0) return TNC_ERR_ARG;
+  const int64_t nr = m, L = n;
+  RowsLayout Ly = rows_layout(nr, sizeof(double));
+  if (wb < Ly.total) return TNC_ERR_WORKSPACE;
+  if (nkeep > nr) nkeep = nr;
+  if (max_sweeps <= 0) max_sweeps = 40;
+  if (max_sweeps > kRowsMaxSweeps) max_sweeps = kRowsMaxSweeps;
+  if (tol <= 0) tol = 1e-7;
+  char* w = (char*)work;
+  double* D = (double*)(w + Ly.d);
+  dfr* Dn = (dfr*)(w + Ly.dn);
+  unsigned* counters = (unsigned*)(w + Ly.counters);
+  SyncWords* sw = (SyncWords*)(w + Ly.sync);
+  double* frob2 = (double*)(w + Ly.frob2);  // [0] of A, [1] of the scaled rows
+  Tdf* W = (Tdf*)Wv;
+  if (cudaMemsetAsync(counters, 0, (kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned), st) != cudaSuccess)
+    return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(info, 0, 4 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
+  if (cudaMemsetAsync(frob2, 0, 2 * sizeof(double), st) != cudaSuccess) return TNC_ERR_CUDA;
+  frob2_kernel<Tin><<<grid1d(nr * L, 256, 152 * 4), 256, 0, st>>>(nr * L, A, frob2);
+  df_widen_kernel<Tin, Tdf><<<grid1d(nr * L, 256), 256, 0, st>>>(nr * L, A, W, frob2);
+  int launched = 2;
+  if (nr > 1) {
+    int h = 8;
+    if (block_rows == 2 || block_rows == 4) h = block_rows;
+    while (h > 2 && (size_t)2 * h * L * sizeof(Tdf) > kMaxHalfBlockBytes) h >>= 1;
+    while (h > 2 && h / 2 >= nr) h >>= 1;
+    if ((size_t)2 * h * L * sizeof(Tdf) > kMaxHalfBlockBytes) return TNC_ERR_ARG;  // rows too long
+    if (int rc = launch_block<Tdf, 1, 256, false>(W, nr, L, h, max_sweeps, tol, frob2 + 1, Dn, counters, sw, info,
+                                                 nkeep, st))
+      return rc;
+    ++launched;
+  }
+  copy_sync_error<<<1, 1, 0, st>>>(sw, info);
+  df_narrow_kernel<Tdf, Tout><<<grid1d(nr * L, 256), 256, 0, st>>>(nr * L, W, frob2);
+  rows_norm_kernel<Tout><<<grid1d(nr * 32, 256), 256, 0, st>>>((const Tout*)Wv, nr, L, D, info);
+  sort_desc_kernel<double><<<grid1d(nr, 128), 128, 0, st>>>(D, nr, order, S);
+  return launch_status(4 + launched);
+}
+
 TNC_DEFINE_SPIN_SETTER(spin_limit_set_rows)
 
 }  // namespace tnc
@@ -607,7 +880,31 @@ extern "C" int tnc_svd_rows(int dtype, int64_t m, int64_t n, const void* A, void
   cudaStream_t st = (cudaStream_t)stream;
   TNC_DISPATCH(dtype, T,
                return svd_rows_impl<T>(m, n, (const T*)A, (T*)W, (typename traits<T>::real*)S, order, max_sweeps,
-                                       tol, block_rows, work, work_bytes, info, st));
+                                       tol, block_rows, INT64_MAX, work, work_bytes, info, st));
+  return TNC_ERR_ARG;
+}
+
+extern "C" int tnc_svd_rows_keep(int dtype, int64_t m, int64_t n, const void* A, void* W, void* S, int64_t* order,
+                                 int max_sweeps, double tol, int block_rows, int64_t nkeep, void* work,
+                                 size_t work_bytes, int* info, void* stream) {
+  if (nkeep < 0) return TNC_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  TNC_DISPATCH(dtype, T,
+               return svd_rows_impl<T>(m, n, (const T*)A, (T*)W, (typename traits<T>::real*)S, order, max_sweeps,
+                                       tol, block_rows, nkeep, work, work_bytes, info, st));
+  return TNC_ERR_ARG;
+}
+
+extern "C" int tnc_svd_rows_df(int dtype, int64_t m, int64_t n, const void* A, void* W, void* S, int64_t* order,
+                               int max_sweeps, double tol, int block_rows, int64_t nkeep, void* work,
+                               size_t work_bytes, int* info, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == TNC_C64)
+    return svd_rows_df_impl<c64, dfc, c128>(m, n, (const c64*)A, W, (double*)S, order, max_sweeps, tol, block_rows,
+                                            nkeep, work, work_bytes, info, st);
+  if (dtype == TNC_F32)
+    return svd_rows_df_impl<float, dfr, double>(m, n, (const float*)A, W, (double*)S, order, max_sweeps, tol,
+                                                block_rows, nkeep, work, work_bytes, info, st);
   return TNC_ERR_ARG;
 }
 

@@ -25,8 +25,10 @@
 // With the FP64 core (core = 1, single-precision storage only) the Jacobi of
 // every truncating bond runs twice: the storage-precision Jacobi above brings
 // the rows of R to orthogonality at the FP32 rounding level, then the rows are
-// widened to FP64 and a one-sided FP64 Jacobi finishes them (tolerances
-// kCoreFp32Tol / kCoreTol: usually one rotating and one checking FP64 sweep);
+// sorted by norm, widened to FP64, and a one-sided FP64 Jacobi finishes them
+// (tolerances kCoreFp32Tol / kCoreTol: usually one rotating and one checking
+// FP64 sweep); rows beyond the FP32 rank plus a margin are rotated against
+// the kept rows only (they are discarded);
 // the singular values, the truncation decision (s / s_max > threshold, at most
 // chi) and U come from the FP64 rows.  The products around the core stay in
 // the storage precision.
@@ -57,7 +59,8 @@ struct Dims {
   std::vector<int64_t> bp;  // applied bonds b_i * D_i
   int64_t max_site = 0, max_r = 0, max_u = 0, max_sv = 0, max_kmin = 0;
   size_t fact = 0;          // largest factorisation / GEMM workspace
-  bool core64 = false;      // FP64 Jacobi finish of the bond cores
+  bool core64 = false;      // FP64-accurate Jacobi finish of the bond cores
+  bool core_df = false;     // ... computed in double-float (else in FP64)
 };
 
 // Tolerances of the two Jacobi stages of an FP64 core (|<w_i, w_j>| <= tol
@@ -74,6 +77,11 @@ struct Dims {
 constexpr double kCoreFp32Tol = 3e-6;
 constexpr int kCoreFp32Sweeps = 14;
 constexpr double kCoreTol = 1e-7;
+// Rows beyond the FP32 stage's retained rank that the FP64 stage still
+// finishes against each other: the FP64 decision may retain a few more (or
+// rank them differently); if it retains any row beyond, the whole finish
+// runs again.
+constexpr int64_t kCoreKeepMargin = 16;
 
 // the FP64 type that finishes the Jacobi of a single-precision core
 inline int core_dtype(int dt) { return dt == TNC_C64 ? TNC_C128 : TNC_F64; }
@@ -103,9 +111,10 @@ int64_t rows_limit(int dt) { return fp32_class(dt) ? 1024 : 512; }
 
 // upper bounds of every buffer over the whole sweep
 int plan(int dt, int n_sites, int64_t d, const int64_t* b, const int64_t* D, int core, Dims& P) {
-  if (core != 0 && core != 1) return TNC_ERR_ARG;
-  if (core == 1 && !fp32_class(dt)) return TNC_ERR_ARG;  // the FP64 core finishes single-precision cores
-  P.core64 = core == 1;
+  if (core != 0 && core != 1 && core != 2) return TNC_ERR_ARG;
+  if (core != 0 && !fp32_class(dt)) return TNC_ERR_ARG;  // the finish is of single-precision cores
+  P.core64 = core != 0;
+  P.core_df = core == 2;
   P.bp.resize(n_sites + 1);
   for (int i = 0; i <= n_sites; ++i) {
     if (b[i] <= 0 || D[i] <= 0) return TNC_ERR_ARG;
@@ -351,6 +360,7 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
   double norm_acc = 1.0;
   std::vector<R> s_host((size_t)P.max_kmin);
   std::vector<double> sd;  // the spectrum the truncation decision reads
+  std::vector<int64_t> ord;  // the FP64 stage's row order
   for (int i = n_sites - 1; i >= 1; --i) {
     const int64_t l = sl[i], r = sr[i], m = d * r, n = l, kmin = m < n ? m : n;
     {  // M = P_i as (d, r, l)
@@ -383,29 +393,67 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
     // the FP64 finish of the core (rows up to the FP64 register limit)
     if (core_path) {
       // an FP32 stage that stopped at its sweep cap hands over to the FP64 stage
+      if (cudaMemcpyAsync(s_host.data(), B.S, (size_t)kmin * sizeof(R), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return TNC_ERR_CUDA;
       if (int stq = device_status(B.info, st); stq && stq != TNC_ERR_NOT_CONVERGED) return stq;
       prof.add(2, svd_flops(kmin, m, cplx));
+      // rows in FP32-norm order, widened; only the rows that can be retained
+      // (the FP32 rank plus a margin) need FP64 orthogonality to every row
+      sd.assign(s_host.begin(), s_host.begin() + kmin);
+      const int64_t k32 = rank_rule<double>(sd, chi, threshold, eps);
+      int64_t nkeep = ((k32 + kCoreKeepMargin + 7) / 8) * 8;
+      if (nkeep > kmin) nkeep = kmin;
       const int cdt = core_dtype(dt);
-      if (int rc = tnc_cast(dt, cdt, kmin * m, B.wbuf, B.w64a, st)) return rc;
+      const int64_t kall = kmin;
+      if (cudaMemcpyAsync(B.kdev, &kall, sizeof(int64_t), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return TNC_ERR_CUDA;
+      if (int rc = tnc_gather_rows(dt, B.wbuf, m, B.order, B.kdev, kmin, nullptr, 0, B.ubuf, st)) return rc;
       if (tnc_svd_rows_workspace_size(cdt, kmin, m, &xb) != TNC_OK || xb > factb) return TNC_ERR_WORKSPACE;
-      prof.begin(3, st);
-      if (int rc = tnc_svd_rows(cdt, kmin, m, B.w64a, B.w64b, B.S64, B.order64, 0,
-                                core_tol > 0 ? core_tol : kCoreTol, block_rows, B.fact, factb, B.info, st))
-        return rc;
-      prof.end(3, st);
-      sd.resize((size_t)kmin);
-      if (cudaMemcpyAsync(sd.data(), B.S64, (size_t)kmin * sizeof(double), cudaMemcpyDeviceToHost, st) !=
-          cudaSuccess)
-        return TNC_ERR_CUDA;
-      int hinfo[2] = {0, 0};
-      if (cudaMemcpyAsync(hinfo, B.info, sizeof(hinfo), cudaMemcpyDeviceToHost, st) != cudaSuccess)
-        return TNC_ERR_CUDA;
-      if (cudaStreamSynchronize(st) != cudaSuccess) return TNC_ERR_CUDA;
-      if (hinfo[0]) return hinfo[0];
-      {  // executed FP64 flops: rotating sweeps, then the checking one
-        const double nn = (double)kmin * kmin * m, sweeps = hinfo[1] > 0 ? hinfo[1] : 1;
-        prof.add(3, ((sweeps - 1.0) * 14.0 + 4.0) * nn / (cplx ? 1.0 : 3.0));
+      double fp64_flops = 0.0;
+      const double tol64 = core_tol > 0 ? core_tol : kCoreTol;
+      for (int attempt = 0; attempt < 2; ++attempt) {
+        if (P.core_df) {
+          prof.begin(3, st);
+          if (int rc = tnc_svd_rows_df(dt, kmin, m, B.ubuf, B.w64b, B.S64, B.order64, 0, tol64, block_rows, nkeep,
+                                       B.fact, factb, B.info, st))
+            return rc;
+          prof.end(3, st);
+        } else {
+          if (int rc = tnc_cast(dt, cdt, kmin * m, B.ubuf, B.w64a, st)) return rc;
+          prof.begin(3, st);
+          if (int rc = tnc_svd_rows_keep(cdt, kmin, m, B.w64a, B.w64b, B.S64, B.order64, 0, tol64, block_rows,
+                                         nkeep, B.fact, factb, B.info, st))
+            return rc;
+          prof.end(3, st);
+        }
+        sd.resize((size_t)kmin);
+        if (cudaMemcpyAsync(sd.data(), B.S64, (size_t)kmin * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess)
+          return TNC_ERR_CUDA;
+        ord.resize((size_t)kmin);
+        if (cudaMemcpyAsync(ord.data(), B.order64, (size_t)kmin * sizeof(int64_t), cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess)
+          return TNC_ERR_CUDA;
+        int hinfo[2] = {0, 0};
+        if (cudaMemcpyAsync(hinfo, B.info, sizeof(hinfo), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+          return TNC_ERR_CUDA;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return TNC_ERR_CUDA;
+        if (hinfo[0]) return hinfo[0];
+        {  // executed arithmetic: rotating sweeps, then the checking one (pairs of kept rows);
+           // FP64 flops, or the FP32 operations of the double-float finish
+          const double pairs = (double)kmin * kmin - (double)(kmin - nkeep) * (kmin - nkeep);
+          const double nn = pairs * m, sweeps = hinfo[1] > 0 ? hinfo[1] : 1;
+          if (P.core_df) fp64_flops += ((sweeps - 1.0) * (cplx ? 44.0 : 15.0) + (cplx ? 24.0 : 6.0)) * nn;
+          else fp64_flops += ((sweeps - 1.0) * 14.0 + 4.0) * nn / (cplx ? 1.0 : 3.0);
+        }
+        // the FP64 decision must retain only rows the FP64 stage finished
+        const int64_t k64 = rank_rule<double>(sd, chi, threshold, eps);
+        bool inside = true;
+        for (int64_t j = 0; j < k64; ++j) inside = inside && ord[(size_t)j] < nkeep;
+        if (inside || nkeep >= kmin) break;
+        nkeep = kmin;  // rerun the whole finish
       }
+      prof.add(3, fp64_flops);
     } else {
       if (cudaMemcpyAsync(s_host.data(), B.S, (size_t)kmin * sizeof(R), cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return TNC_ERR_CUDA;

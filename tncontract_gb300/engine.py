@@ -37,15 +37,23 @@ from . import _ops
 
 _DT = {"fp32": (torch.complex64, torch.float32), "fp64": (torch.complex128, torch.float64),
        "mixed": (torch.complex64, torch.float32)}
+# The finish of the "mixed" precision's bond cores: "df" runs it in
+# double-float arithmetic on the FP32 pipe (tnc_svd_rows_df), "fp64" in FP64.
+MIXED_CORE = "df"
 # precision -> how the native sweep factors each bond core
-CORE = {"fp32": L.CORE_STORAGE, "fp64": L.CORE_STORAGE, "mixed": L.CORE_FP64}
+CORE = {"fp32": L.CORE_STORAGE, "fp64": L.CORE_STORAGE, "mixed": L.CORE_DF}
+
+
+def mixed_core(precision):
+    """The ``core`` argument of a precision: MIXED_CORE for "mixed", else None."""
+    return MIXED_CORE if precision == "mixed" else None
 
 
 def compute_dtype(precision, is_complex):
     """Storage dtype of a precision: "fp64" complex128 / float64; "fp32" and
     "mixed" complex64 / float32 ("mixed" finishes every bond core's Jacobi
-    in FP64 and decides the truncation on the FP64 singular values, see
-    ``apply_compress_native``)."""
+    to FP64-level orthogonality, in double-float arithmetic, and decides the
+    truncation on those singular values, see ``apply_compress_native``)."""
     return _DT[precision][0 if is_complex else 1]
 
 
@@ -130,9 +138,9 @@ def _check_info(info):
         raise _ops.LinAlgError("SVD did not converge (status %d)" % st)
 
 
-# FP64 core finish (the "mixed" precision of single-precision sites): the
-# tolerances of the storage-precision Jacobi stage and of the FP64 stage, as
-# in the native sweep (tnc_sweep.cu)
+# Core finish (the "mixed" precision of single-precision sites): the
+# tolerances of the storage-precision Jacobi stage and of the finishing
+# (double-float or FP64) stage, as in the native sweep (tnc_sweep.cu)
 CORE_FP32_TOL, CORE_FP32_SWEEPS, CORE_FP64_TOL = 3e-6, 14, 1e-7
 _WIDE = {torch.float32: torch.float64, torch.complex64: torch.complex128}
 
@@ -153,14 +161,20 @@ def _factor_full(M, core=None):
     m, n = M.shape
     R = _ops.qr_r(M, adjoint=True)                                         # min(m, n) x m
     wide = _WIDE.get(M.dtype)
-    if core == "fp64" and wide is not None and m <= _rows_limit(wide):
+    if core in ("fp64", "df") and wide is not None and m <= _rows_limit(wide):
         # FP32 Jacobi to near its rounding floor (a stall is handed over), then
-        # the FP64 Jacobi finishes the widened rows; S, the rank decision and U
-        # come from the FP64 rows, U is stored back in the sites' precision
+        # the double-float (or FP64) Jacobi finishes the rows; S, the rank
+        # decision and U come from the finished rows, U is stored back in the
+        # sites' precision
         W32, _s, _o, info = _ops.svd_rows(R, max_sweeps=CORE_FP32_SWEEPS, tol=CORE_FP32_TOL)
         if int(info[0].item()) not in (L.OK, L.ERR_NOT_CONVERGED):
             _check_info(info)
-        W, S, order, info = _ops.svd_rows(_ops.cast(W32, wide), tol=CORE_FP64_TOL)
+        if core == "df":
+            kall = torch.tensor([W32.shape[0]], dtype=torch.int64, device=W32.device)
+            rows = _ops.gather_rows(W32, _o, kall, W32.shape[0])                # FP32 norm order
+            W, S, order, info = _ops.svd_rows_df(rows, tol=CORE_FP64_TOL)
+        else:
+            W, S, order, info = _ops.svd_rows(_ops.cast(W32, wide), tol=CORE_FP64_TOL)
         _check_info(info)
 
         def factors(k, kdev):
@@ -399,11 +413,12 @@ def apply_compress_native(sites, mpo, chi, threshold=1e-15, log_norm_in=0.0, sta
     fraction of the squared singular values, bonds left to right) when
     ``stats`` is given.  ``profile``: a ctypes array of 12 doubles
     accumulating per-op CUDA-event time, calls and algorithmic flops (QR,
-    R-only QR, Jacobi, its FP64 finish), or None.  ``core``: "fp64" finishes
-    the Jacobi of every bond core in FP64 and takes the spectrum, the
+    R-only QR, Jacobi, its finish), or None.  ``core``: "df" (double-float
+    arithmetic on the FP32 pipe) or "fp64" finishes the Jacobi of every bond
+    core to FP64-level orthogonality and takes the spectrum, the
     truncation decision and U from it (single-precision sites only; the
     "mixed" precision), None / "storage" factors in the storage precision;
-    ``core_tol``: the FP64 Jacobi's tolerance (0: its default)."""
+    ``core_tol``: the finishing Jacobi's tolerance (0: its default)."""
     import ctypes as C
     N = len(sites)
     dt = sites[0].dtype
@@ -415,7 +430,7 @@ def apply_compress_native(sites, mpo, chi, threshold=1e-15, log_norm_in=0.0, sta
     b_arr = (C.c_int64 * (N + 1))(*bonds)
     m_arr = (C.c_int64 * (N + 1))(*mbonds)
     code = _ops.code(dt)
-    core_code = {None: L.CORE_STORAGE, "storage": L.CORE_STORAGE, "fp64": L.CORE_FP64}[core]
+    core_code = {None: L.CORE_STORAGE, "storage": L.CORE_STORAGE, "fp64": L.CORE_FP64, "df": L.CORE_DF}[core]
     sz = C.c_size_t()
     L.check("tnc_sweep_workspace_size",
             L.lib().tnc_sweep_workspace_size(code, N, d, b_arr, m_arr, core_code, C.byref(sz)))
@@ -461,7 +476,7 @@ def apply_compress_host(sites, mpo, chi, precision="mixed", threshold=1e-15, sta
     dtype.  On the current stream the inputs are copied to the device,
     balanced (``balance``) and cast to the storage dtype of ``precision``,
     the sweep runs as one native call (``apply_compress_native``; "mixed"
-    finishes every bond core in FP64), and the result comes back as host
+    finishes every bond core, ``MIXED_CORE``), and the result comes back as host
     arrays of the input's precision class (complex128 / float64 for double
     input) with the state's norm in the first site, as
     ``MatrixProductState.svd_compress`` leaves it (onedim_core.py:463-484)."""
@@ -477,7 +492,7 @@ def apply_compress_host(sites, mpo, chi, precision="mixed", threshold=1e-15, sta
     st = stats if stats is not None else SweepStats()
     out = apply_compress_native([_ops.cast(a, dt) for a in bal], [_ops.cast(w, dt) for w in d_mpo], chi,
                                 threshold=threshold, log_norm_in=log_norm, stats=st,
-                                core="fp64" if precision == "mixed" else None)
+                                core=mixed_core(precision))
     res = [_ops.cast(o, out_dt) for o in out]
     if not st.norm_folded and abs(st.log_norm) < 700:
         # the factor did not fit the storage type; it fits the output's

@@ -78,7 +78,7 @@ def config5_inputs(N=128, d=2, chi=512, seed=5):
 def config5(sites, mpo, chi=512, dw_tol=1e-8, precision="mixed", model=None):
     """One apply + compress sweep of config 5 on the device; returns (sites,
     seconds, RankStats, SweepStats).  ``precision``: "fp32", "mixed" (float32
-    sites, every bond core finished by the FP64 Jacobi) or "fp64"."""
+    sites, every bond core finished by the double-float Jacobi) or "fp64"."""
     dt = E.compute_dtype(precision, False)
     bal, ln = E.balance(sites)
     S, Mo = E.to_sites(bal, dt), E.to_sites(mpo, dt)
@@ -86,7 +86,7 @@ def config5(sites, mpo, chi=512, dw_tol=1e-8, precision="mixed", model=None):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     out = E.apply_compress(S, Mo, chi, log_norm_in=ln, dw_tol=dw_tol, rank_model=model, rank_stats=rs, stats=st,
-                           core="fp64" if precision == "mixed" else None)
+                           core=E.mixed_core(precision))
     torch.cuda.synchronize()
     return out, time.perf_counter() - t0, rs, st
 
