@@ -45,8 +45,9 @@ METRIC = "MPO-MPS apply+compress sweeps/s at chi=256 (TFIM D=3, N=64, d=2, compl
 # shape, from ncu captures of their Jacobi kernels at that shape (the matrix
 # once in and once out; the working set stays in L2): the FP32 Jacobi on the
 # 512 x 512 complex64 factor 2.410 MB read + 0.488 MB written, the FP64 finish
-# on the 512 x 512 complex128 rows 5.191 MB + 0.435 MB; absent = not captured.
-TRAFFIC_PER_CALL = {"tnc_svd_rows": 2.898e6, "tnc_svd_rows_fp64_finish": 5.626e6}
+# on the 512 x 512 complex128 rows 5.191 MB + 0.435 MB, the double-float finish
+# on the 512 x 512 DF rows 4.279 MB + 0.052 MB; absent = not captured.
+TRAFFIC_PER_CALL = {"tnc_svd_rows": 2.898e6, "tnc_svd_rows_fp64_finish": 5.626e6, "tnc_svd_rows_df": 4.331e6}
 # the bond-core finish of the mixed precision, by its arithmetic
 FINISH_OP = {"df": "tnc_svd_rows_df", "fp64": "tnc_svd_rows_fp64_finish"}
 # FP32 pipe: 152 SMs x 128 lanes x 2.07 GHz operations/s (x 2 for FMA flops)
@@ -73,8 +74,8 @@ def parse():
                         "config 5 (XXZ D=5, N=128, chi=512, learned rank against the plain and FP64 sweeps)")
     p.add_argument("--instances", type=int, default=512, help="instances of the uneven batch")
     p.add_argument("--micro", default=None,
-                   help="time one native op instead: svd:MxN:DT, qr:MxN:DT or gemm:MxNxK:DT "
-                        "(DT in f32,f64,c64,c128); used for kernel profiling")
+                   help="time one native op instead: svd:MxN:DT, qr:MxN:DT, gemm:MxNxK:DT, svdrows[H]:MxN:DT "
+                        "or dffinish:MxN:DT (DT in f32,f64,c64,c128); used for kernel profiling")
     return p.parse_args()
 
 
@@ -111,6 +112,18 @@ def run_micro(args):
         Cm = torch.empty((dims[0], dims[1]), dtype=A.dtype, device="cuda")
         tc = {"gemm": None, "gemmtc": True, "gemmsimt": False}[op]
         fn = lambda: _ops.gemm(0, 0, dims[0], dims[1], dims[2], A, dims[2], B, dims[1], Cm, dims[1], tc=tc)
+    elif op == "dffinish":
+        # the mixed sweep's bond-core finish: FP32 Jacobi rows (3e-6, sorted by
+        # norm) orthogonalised in double-float to 1e-7
+        A = mat(*dims)
+        W32, _s, o32, _i = _ops.svd_rows(A, max_sweeps=14, tol=3e-6)
+        kall = torch.tensor([dims[0]], dtype=torch.int64, device="cuda")
+        rows = _ops.gather_rows(W32, o32, kall, dims[0])
+
+        def fn():
+            r = _ops.svd_rows_df(rows, tol=1e-7)
+            infos.append(r[3])
+            return r
     elif op.startswith("svdrows"):
         A = mat(*dims)
         h = int(op[7:]) if len(op) > 7 else None
@@ -132,7 +145,8 @@ def run_micro(args):
     _ops.PROFILE = None
     name = {"svd": "tnc_svd", "qr": "tnc_qr", "qrr": "tnc_qr_r", "qrrh": "tnc_qr_r",
             "gemmsimt": "tnc_gemm", "gemmtc": "tnc_gemm_tc",
-            "gemm": "tnc_gemm_tc" if "tnc_gemm_tc" in summ else "tnc_gemm"}.get(op, "tnc_svd_rows")
+            "gemm": "tnc_gemm_tc" if "tnc_gemm_tc" in summ else "tnc_gemm",
+            "dffinish": "tnc_svd_rows_df"}.get(op, "tnc_svd_rows")
     n, ms, fl = summ[name]
     extra = {}
     if infos:
