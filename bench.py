@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batch", type=int, default=12, help="independent instances per GPU")
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
+    p.add_argument("--block-rows", type=int, default=0, choices=[0, 2, 4, 8, 16],
+                   help="Jacobi half-block height of the sweep (0: the library's default, 8)")
     p.add_argument("--core", default="df", choices=["df", "fp64"],
                    help="the mixed precision's bond-core finish: double-float or FP64 arithmetic")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 engine arm")
@@ -336,7 +338,7 @@ def run_ours(args):
         def job():
             st = E.SweepStats()
             out[b] = E.apply_compress_native(batch[b], mpo, chi, log_norm_in=log_norms[b], profile=prof,
-                                             stats=st, core=precision_core)
+                                             stats=st, core=precision_core, block_rows=args.block_rows)
             stats[b] = st
         return job
 
@@ -510,6 +512,7 @@ def run_ours(args):
             "dtype": dtype_name, "data": "synthetic (seeded random MPS, TFIM MPO)",
             "config": {"workload": "tfim_apply_svd_compress", "path": path, "precision": args.precision,
                        "batch_per_gpu": B, "nsites": N, "phys_dim": PHYS, "mpo_bond": MPO_D, "chi": chi,
+                       "block_rows": args.block_rows or 8,
                        "input_dtype": "complex128", "parallelism": "replicas" if world > 1 else "single",
                        "scheduling": "K steps x %d sweeps as one work queue on %d CUDA streams (continuous "
                                      "batching), workers admitted %d ms apart, each sweep one native call"

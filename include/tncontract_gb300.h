@@ -273,8 +273,14 @@ int tnc_svd_noalloc(int dtype, int64_t m, int64_t n, const void *A,
  * A, rows order[:k] of W are S_k V_k^H and U_k = A (S_k V_k^H)^H S_k^-2; for
  * a tall A they are S_k U_k^H and S_k V_k^H = U_k^H A.  block_rows (2, 4, 8,
  * or 16 for rows up to 512 of types up to 8 bytes; anything else selects 8)
- * is the half-block height, chosen per shape by the caller's autotuner.
+ * is the half-block height of the row-by-row rotation kernel, chosen per
+ * shape by the caller's autotuner (0: 8); TNC_ROWS_GRAM selects, for F32 /
+ * C64 rows, the Gram-form block update: each half-block pair's rotations
+ * run on its 16 x 16 Gram matrix and are applied to the rows as one 16 x 16
+ * product (same rotations, GEMM-shaped work; 8-row half-blocks, the
+ * row-by-row kernel where fewer rows need smaller ones).
  * max(m,n) <= 1024 (512 for F64/C128).  info as for tnc_svd. */
+enum { TNC_ROWS_GRAM = 32 };
 int tnc_svd_rows_workspace_size(int dtype, int64_t m, int64_t n, size_t *bytes);
 int tnc_svd_rows(int dtype, int64_t m, int64_t n, const void *A, void *W,
                  void *S, int64_t *order, int max_sweeps, double tol,

@@ -20,8 +20,11 @@ def rnd(rng, shape, dt):
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64, np.complex64, np.complex128])
 @pytest.mark.parametrize("shape", [(2, 2), (3, 40), (40, 3), (33, 65), (96, 200), (260, 120), (512, 768)])
-@pytest.mark.parametrize("block_rows", [None, 16])
+@pytest.mark.parametrize("block_rows", [None, 8, 16, 32])
 def test_svd_rows(gpu, dt, shape, block_rows):
+    """block_rows: None the autotuner's choice, 8 / 16 the row-by-row
+    rotation kernel, 32 (TNC_ROWS_GRAM) the Gram-form block update (single
+    precision; the other types run the row-by-row kernel)."""
     from tncontract_gb300 import _ops
     if np.dtype(dt).itemsize * (2 if np.iscomplexobj(np.zeros(0, dt)) else 1) >= 16 and max(shape) > 512:
         pytest.skip("FP64 complex rows above 512 use the accumulating SVD")

@@ -17,6 +17,7 @@ F32, F64, C64, C128 = 0, 1, 2, 3
 OK, ERR_ARG, ERR_NOT_CONVERGED, ERR_NONFINITE, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_TOO_LARGE = range(8)
 OP_N, OP_T, OP_C, OP_R = 0, 1, 2, 3
 CORE_STORAGE, CORE_FP64, CORE_DF = 0, 1, 2
+ROWS_GRAM = 32  # block_rows code of the Gram-form Jacobi update
 
 _vp = C.c_void_p
 _i64 = C.c_int64

@@ -673,7 +673,7 @@ def truncation_rank(S, chi, threshold, relative, with_smax=False, kdev_out=None)
 
 _TUNE = {}            # (dtype, m, n) -> half-block height chosen by the autotuner
 _TUNE_LOCK = threading.Lock()
-TUNE_CANDIDATES = (4, 8)
+TUNE_CANDIDATES = (L.ROWS_GRAM, 4, 8)
 
 
 def _svd_rows_call(M, W, S, order, info, h, max_sweeps, tol):
