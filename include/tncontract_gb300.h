@@ -300,6 +300,20 @@ int tnc_svd_rows_keep(int dtype, int64_t m, int64_t n, const void *A, void *W,
                       int block_rows, int64_t nkeep, void *work,
                       size_t work_bytes, int *info, void *stream);
 
+/* The rows of src (m x L) in decreasing-norm order: dst[i] = src[order[i]],
+ * stable (equal norms keep their order; a NaN norm ranks last), rank[j] =
+ * the dst row of src row j.  norms2: m doubles of the caller's device memory
+ * (the squared norms).  src and dst must not overlap.  The sweep sorts each
+ * bond matrix's rows before the R-only QR of M^H (a static column pivoting
+ * of that QR: the Jacobi on R then needs fewer sweeps) -- part of the
+ * truncating SVD of left_canonise, onedim_core.py:317-343. */
+int tnc_sort_rows(int dtype, int64_t m, int64_t L, const void *src, void *dst,
+                  int64_t *order, int64_t *rank, double *norms2, void *stream);
+/* dst[i] = src[idx[i]] for i < n (rows of length L; device idx) -- e.g. the
+ * inverse of tnc_sort_rows with idx = rank.  src and dst must not overlap. */
+int tnc_permute_rows(int dtype, int64_t n, int64_t L, const void *src,
+                     const int64_t *idx, void *dst, void *stream);
+
 /* The extended-precision finish of single-precision rows, in double-float
  * arithmetic on the FP32 pipe (a real number as an unevaluated pair of
  * floats, about 48 significant bits; error-free TwoSum / TwoProd and Dot2

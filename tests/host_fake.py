@@ -92,6 +92,18 @@ def _gather(W, order, kdev, kmax, S=None, mode=0):
     return (rows.conj().T / S[:k].to(W.dtype)[None, :]).contiguous()
 
 
+def _sort_rows(M):
+    nrm = (M.abs() ** 2).sum(1).double()
+    order = torch.from_numpy(np.argsort(-nrm.numpy(), kind="stable").copy())
+    rank = torch.empty_like(order)
+    rank[order] = torch.arange(len(order))
+    return M[order].contiguous(), order, rank
+
+
+def _permute_rows(X, idx):
+    return X[idx].contiguous()
+
+
 def _copy2d(src, rows, cols, lds, dst, ldd, src_off=0, dst_off=0):
     s = src.reshape(-1)
     d = dst.reshape(-1)
@@ -214,6 +226,8 @@ PATCH = {
     "gemm": _gemm,
     "svd_rows": _svd_rows,
     "gather_rows": _gather,
+    "sort_rows": _sort_rows,
+    "permute_rows": _permute_rows,
     "copy2d": _copy2d,
     "mps_mpo_site": _mps_mpo_site,
     "scale_rows": _scale_rows,

@@ -253,3 +253,24 @@ def test_engine_inner_product(gpu):
     da = E.to_sites(a, torch.complex128)
     db = E.to_sites(b, torch.complex128)
     assert abs(E.inner_product(da, db) - O.inner_product(a, b)) < 1e-10 * abs(O.inner_product(a, b))
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.complex64, np.float64, np.complex128])
+def test_sort_rows(gpu, dt):
+    """tnc_sort_rows: decreasing norm, equal norms in their original order, a
+    NaN row last; tnc_permute_rows with the rank restores the rows exactly."""
+    from tncontract_gb300 import _ops
+    rng = np.random.default_rng(3)
+    A = rnd(rng, (37, 19), dt)
+    A[9] = A[5]
+    A[20] = 0
+    A[30, 2] = np.nan
+    Ms, order, rank = _ops.sort_rows(torch.from_numpy(A).cuda())
+    o, r = order.cpu().numpy(), rank.cpu().numpy()
+    nrm = (np.abs(A.astype(np.complex128)) ** 2).sum(1)
+    assert list(o) == list(np.argsort(-nrm, kind="stable"))
+    assert o[-1] == 30 and o[-2] == 20
+    assert np.array_equal(r[o], np.arange(37))
+    assert np.array_equal(Ms.cpu().numpy(), A[o], equal_nan=True)
+    back = _ops.permute_rows(Ms, rank).cpu().numpy()
+    assert np.array_equal(back, A, equal_nan=True)

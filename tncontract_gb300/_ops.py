@@ -738,6 +738,28 @@ def svd_rows(M, max_sweeps=0, tol=0.0, block_rows=None):
     return W, S, order, info
 
 
+def sort_rows(M):
+    """(M', order, rank): M's rows in decreasing-norm order (``tnc_sort_rows``;
+    M'[i] = M[order[i]], M[j] = M'[rank[j]])."""
+    M = M.contiguous()
+    m, L = M.shape
+    out = empty((m, L), M.dtype)
+    order = torch.empty(m, dtype=torch.int64, device=device())
+    rank = torch.empty(m, dtype=torch.int64, device=device())
+    norms2 = torch.empty(m, dtype=torch.float64, device=device())
+    _call("tnc_sort_rows", code(M.dtype), m, L, _p(M), _p(out), _p(order), _p(rank), _p(norms2), _stream())
+    return out, order, rank
+
+
+def permute_rows(X, idx):
+    """dst[i] = X[idx[i]] (``tnc_permute_rows``)."""
+    X = X.contiguous()
+    n = int(idx.shape[0])
+    out = empty((n, X.shape[1]), X.dtype)
+    _call("tnc_permute_rows", code(X.dtype), n, X.shape[1], _p(X), _p(idx), _p(out), _stream())
+    return out
+
+
 def svd_rows_df(M, max_sweeps=0, tol=0.0, block_rows=0, nkeep=None):
     """Double-float Jacobi of the rows of a wide single-precision M
     (``tnc_svd_rows_df``): returns (W, S, order, info) as ``svd_rows`` of M

@@ -15,23 +15,27 @@
 //
 // Per site of the QR left sweep:   Q, R = qr(P_i as (d l) x r);  P_i = Q;
 //                                  P_{i+1} <- (R / |R|) P_{i+1}.
-// Per site of the SVD right sweep: M = P_i as (d r) x l;  R = qr_r(M^H);
-//                                  Jacobi on the rows of R (rotated rows =
-//                                  S U^H of M);  k from the reference's rule
-//                                  (s / s_max > threshold, at most chi) capped
-//                                  at the rounding-noise floor 4 eps |M|_F;
-//                                  U = normalised rows;  S V^H = U^H M;
-//                                  P_i = U;  P_{i-1} <- P_{i-1} (S V^H)^T / s_max.
-// With the FP64 core (core = 1, single-precision storage only) the Jacobi of
-// every truncating bond runs twice: the storage-precision Jacobi above brings
-// the rows of R to orthogonality at the FP32 rounding level, then the rows are
-// sorted by norm, widened to FP64, and a one-sided FP64 Jacobi finishes them
-// (tolerances kCoreFp32Tol / kCoreTol: usually one rotating and one checking
-// FP64 sweep); rows beyond the FP32 rank plus a margin are rotated against
-// the kept rows only (they are discarded);
+// Per site of the SVD right sweep: M = P_i as (d r) x l, its rows sorted by
+//                                  norm (M' = Pi M: a static column pivoting
+//                                  of the QR below, fewer Jacobi sweeps);
+//                                  R = qr_r(M'^H);  Jacobi on the rows of R
+//                                  (rotated rows = S U'^H of M');  k from the
+//                                  reference's rule (s / s_max > threshold, at
+//                                  most chi) capped at the rounding-noise floor
+//                                  4 eps |M|_F;  U' = normalised rows;
+//                                  S V^H = U'^H M';  P_i = U = Pi^T U';
+//                                  P_{i-1} <- P_{i-1} (S V^H)^T / s_max.
+// With a finishing core (core = 1 FP64, core = 2 double-float; single-
+// precision storage only) the Jacobi of every truncating bond runs twice: the
+// storage-precision Jacobi above brings the rows of R to orthogonality at the
+// FP32 rounding level, then the rows are sorted by norm and a one-sided
+// Jacobi in FP64 (widened rows) or in double-float arithmetic on the FP32
+// pipe finishes them (tolerances kCoreFp32Tol / kCoreTol: usually one
+// rotating and one checking sweep); rows beyond the FP32 rank plus a margin
+// are rotated against the kept rows only (they are discarded);
 // the singular values, the truncation decision (s / s_max > threshold, at most
-// chi) and U come from the FP64 rows.  The products around the core stay in
-// the storage precision.
+// chi) and U come from the finished rows.  The products around the core stay
+// in the storage precision.
 // All buffers are carved from one caller workspace sized for the un-truncated
 // bond dimensions (tnc_sweep_workspace_size); nothing is allocated.
 #include "tnc_common.cuh"
@@ -57,7 +61,7 @@ struct Carve {
 
 struct Dims {
   std::vector<int64_t> bp;  // applied bonds b_i * D_i
-  int64_t max_site = 0, max_r = 0, max_u = 0, max_sv = 0, max_kmin = 0;
+  int64_t max_site = 0, max_r = 0, max_u = 0, max_sv = 0, max_kmin = 0, max_m = 0;
   size_t fact = 0;          // largest factorisation / GEMM workspace
   bool core64 = false;      // FP64-accurate Jacobi finish of the bond cores
   bool core_df = false;     // ... computed in double-float (else in FP64)
@@ -137,6 +141,7 @@ int plan(int dt, int n_sites, int64_t d, const int64_t* b, const int64_t* D, int
     }
     // SVD right sweep: M (d r) x l, R of M^H kmin x m, U m x kmin, S V^H kmin x l
     const int64_t m = d * r, n = l, kmin = m < n ? m : n;
+    P.max_m = m > P.max_m ? m : P.max_m;
     if (tnc_qr_r_workspace_size(dt, m, n, 1, &x) != TNC_OK) return TNC_ERR_ARG;
     f = x > f ? x : f;
     // the rows path runs whenever the truncated row count is within the
@@ -175,6 +180,9 @@ struct Buffers {
   double* S64 = nullptr;
   int64_t* order64 = nullptr;
   int64_t* order;
+  void* mpiv;                      // the bond matrix with its rows sorted by norm
+  int64_t *porder, *prank;         // that sort and its inverse
+  double* pnorm2;
   int64_t* kdev;
   double* dnorm;
   int* info;
@@ -190,6 +198,10 @@ size_t carve(Carve& c, int n_sites, int64_t d, const Dims& P, size_t es, size_t 
   B.svbuf = c.take((size_t)P.max_sv * es);
   B.S = c.take((size_t)P.max_kmin * rs);
   B.order = (int64_t*)c.take((size_t)P.max_kmin * sizeof(int64_t));
+  B.mpiv = c.take((size_t)P.max_site * es);
+  B.porder = (int64_t*)c.take((size_t)P.max_m * sizeof(int64_t));
+  B.prank = (int64_t*)c.take((size_t)P.max_m * sizeof(int64_t));
+  B.pnorm2 = (double*)c.take((size_t)P.max_m * sizeof(double));
   B.kdev = (int64_t*)c.take(sizeof(int64_t));
   B.dnorm = (double*)c.take(sizeof(double));
   B.info = (int*)c.take(4 * sizeof(int));
@@ -369,6 +381,14 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
       if (int rc = tnc_permute(dt, B.slot[i], B.scratch, 3, shp, perm, 0, st)) return rc;
     }
     const void* M = B.scratch;
+    const bool rows_path = m <= rows_limit(dt);
+    // rows path: M's rows in decreasing-norm order (they are graded by the
+    // previous bond's spectrum), a static column pivoting of the QR of M^H
+    // that cuts the Jacobi's sweeps; U's rows are put back in order below
+    if (rows_path) {
+      if (int rc = tnc_sort_rows(dt, m, n, B.scratch, B.mpiv, B.porder, B.prank, B.pnorm2, st)) return rc;
+      M = B.mpiv;
+    }
     size_t xb = 0;
     if (tnc_qr_r_workspace_size(dt, m, n, 1, &xb) != TNC_OK || xb > factb) return TNC_ERR_WORKSPACE;
     prof.begin(1, st);
@@ -376,7 +396,6 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
     prof.end(1, st);
     if (int stq = device_status(B.info, st)) return stq;
     prof.add(1, qr_flops(n, m, cplx));
-    const bool rows_path = m <= rows_limit(dt);
     prof.begin(2, st);
     const bool core_path = P.core64 && rows_path && m <= core_rows_limit(dt);
     if (rows_path) {
@@ -494,10 +513,15 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
     if (int rc = gemm_any(dt, TNC_OP_C, TNC_OP_N, k, n, m, 1.0, B.ubuf, k, 0, M, n, 0, B.svbuf, n, 0, 1, B.fact, factb,
                           st))
       return rc;
+    const void* U = B.ubuf;
+    if (rows_path) {  // U's rows back in M's order (wbuf is free once U is formed)
+      if (int rc = tnc_permute_rows(dt, m, k, B.ubuf, B.prank, B.wbuf, st)) return rc;
+      U = B.wbuf;
+    }
     {  // P_i = U as (d, r, k) -> (d, k, r)
       const int64_t shp[3] = {d, r, k};
       const int perm[3] = {0, 2, 1};
-      if (int rc = tnc_permute(dt, B.ubuf, B.slot[i], 3, shp, perm, 0, st)) return rc;
+      if (int rc = tnc_permute(dt, U, B.slot[i], 3, shp, perm, 0, st)) return rc;
     }
     sl[i] = k;
     // P_{i-1} <- P_{i-1} (S V^H)^T / s_max  ((d lp) x k)

@@ -159,8 +159,16 @@ def _factor_full(M, core=None):
     sweeps on graded matrices (Drmac & Veselic 2008).  Longer columns run
     the accumulating SVD on the same R (its VH rows are then U^H of M)."""
     m, n = M.shape
-    R = _ops.qr_r(M, adjoint=True)                                         # min(m, n) x m
     wide = _WIDE.get(M.dtype)
+    rank = None
+    if m <= _rows_limit(M.dtype):
+        # rows in decreasing-norm order (a static column pivoting of the QR of
+        # M^H: fewer Jacobi sweeps); U's rows go back in M's order at the end
+        M, _order, rank = _ops.sort_rows(M)
+    R = _ops.qr_r(M, adjoint=True)                                         # min(m, n) x m
+
+    def unsort(U):
+        return U if rank is None else _ops.permute_rows(U, rank)
     if core in ("fp64", "df") and wide is not None and m <= _rows_limit(wide):
         # FP32 Jacobi to near its rounding floor (a stall is handed over), then
         # the double-float (or FP64) Jacobi finishes the rows; S, the rank
@@ -181,7 +189,7 @@ def _factor_full(M, core=None):
             U = _ops.cast(_ops.gather_rows(W, order, kdev, k, S=S, mode=1), M.dtype)   # m x k
             SV = _ops.empty((k, n), M.dtype)
             _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)     # U^H M
-            return U, SV
+            return unsort(U), SV
         return S, factors
     if m <= _rows_limit(M.dtype):
         W, S, order, info = _ops.svd_rows(R)                               # W rows = S U^H
@@ -191,7 +199,7 @@ def _factor_full(M, core=None):
             U = _ops.gather_rows(W, order, kdev, k, S=S, mode=1)          # m x k
             SV = _ops.empty((k, n), M.dtype)
             _ops.gemm(L.OP_C, L.OP_N, k, n, m, U, k, M, n, SV, n)         # U^H M
-            return U, SV
+            return unsort(U), SV
         return S, factors
     _u, S, VH = _ops.svd(R)                                                # VH rows = U^H of M
 
