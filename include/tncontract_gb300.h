@@ -300,6 +300,18 @@ int tnc_svd_rows_keep(int dtype, int64_t m, int64_t n, const void *A, void *W,
                       int block_rows, int64_t nkeep, void *work,
                       size_t work_bytes, int *info, void *stream);
 
+/* tnc_svd_rows as the first stage of a finished core: the sweeps also stop
+ * (status TNC_OK, info[3] = 1) after the first sweep in which no rotation
+ * met a relative off-diagonal |<w_i, w_j>| / (|w_i| |w_j|) above stop_tol,
+ * instead of running on to a sweep without any rotation above tol -- the
+ * finishing stage (tnc_svd_rows_df / tnc_svd_rows_keep) takes the rows from
+ * there and confirms their orthogonality itself.  stop_tol = 0 is
+ * tnc_svd_rows. */
+int tnc_svd_rows_stage(int dtype, int64_t m, int64_t n, const void *A, void *W,
+                       void *S, int64_t *order, int max_sweeps, double tol,
+                       double stop_tol, int block_rows, void *work,
+                       size_t work_bytes, int *info, void *stream);
+
 /* The rows of src (m x L) in decreasing-norm order: dst[i] = src[order[i]],
  * stable (equal norms keep their order; a NaN norm ranks last), rank[j] =
  * the dst row of src row j.  norms2: m doubles of the caller's device memory

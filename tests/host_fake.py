@@ -84,6 +84,10 @@ def _svd_rows(M, max_sweeps=0, tol=0.0):
             torch.arange(len(s), dtype=torch.int64), torch.zeros(4, dtype=torch.int32))
 
 
+def _svd_rows_stage(M, max_sweeps, tol, stop_tol, block_rows=0):
+    return _svd_rows(M, max_sweeps, tol)
+
+
 def _gather(W, order, kdev, kmax, S=None, mode=0):
     k = min(int(kdev.reshape(-1)[0]), kmax)
     rows = W[order[:k]]
@@ -225,6 +229,7 @@ PATCH = {
     "truncation_rank": _trunc,
     "gemm": _gemm,
     "svd_rows": _svd_rows,
+    "svd_rows_stage": _svd_rows_stage,
     "gather_rows": _gather,
     "sort_rows": _sort_rows,
     "permute_rows": _permute_rows,

@@ -75,6 +75,7 @@ SIGNATURES = {
     "tnc_svd_rows_workspace_size": [_int, _i64, _i64, _psz],
     "tnc_svd_rows": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _vp, C.c_size_t, _vp, _vp],
     "tnc_svd_rows_keep": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _i64, _vp, C.c_size_t, _vp, _vp],
+    "tnc_svd_rows_stage": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _dbl, _int, _vp, C.c_size_t, _vp, _vp],
     "tnc_sort_rows": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _vp],
     "tnc_permute_rows": [_int, _i64, _i64, _vp, _vp, _vp, _vp],
     "tnc_svd_rows_df": [_int, _i64, _i64, _vp, _vp, _vp, _vp, _int, _dbl, _int, _i64, _vp, C.c_size_t, _vp, _vp],

@@ -738,6 +738,25 @@ def svd_rows(M, max_sweeps=0, tol=0.0, block_rows=None):
     return W, S, order, info
 
 
+def svd_rows_stage(M, max_sweeps, tol, stop_tol, block_rows=0):
+    """``svd_rows`` as the first stage of a finished core
+    (``tnc_svd_rows_stage``): also stops after the first sweep without a
+    rotation above ``stop_tol`` (info[3] = 1)."""
+    M = M.contiguous()
+    m, n = M.shape
+    nr, Lr = min(m, n), max(m, n)
+    W = empty((nr, Lr), M.dtype)
+    S = empty((nr,), real_dtype(M.dtype))
+    order = torch.empty(nr, dtype=torch.int64, device=device())
+    info = torch.empty(4, dtype=torch.int32, device=device())
+    sz = C.c_size_t()
+    _call("tnc_svd_rows_workspace_size", code(M.dtype), m, n, C.byref(sz))
+    ws = workspace(sz.value)
+    _call("tnc_svd_rows_stage", code(M.dtype), m, n, _p(M), _p(W), _p(S), _p(order), int(max_sweeps), float(tol),
+          float(stop_tol), int(block_rows), _p(ws), sz.value, _p(info), _stream())
+    return W, S, order, info
+
+
 def sort_rows(M):
     """(M', order, rank): M's rows in decreasing-norm order (``tnc_sort_rows``;
     M'[i] = M[order[i]], M[j] = M'[rank[j]])."""

@@ -33,6 +33,11 @@
 
 namespace tnc {
 
+// sweep cap; the counter words hold a rotation count per sweep, then a count
+// of the rotations above the stage-stop tolerance per sweep, then one step
+// counter per half-block
+constexpr int kRowsMaxSweeps = 100;
+
 __device__ __forceinline__ void circle_pair(int64_t np, int64_t r, int64_t i, int64_t& p, int64_t& q) {
   const int64_t mod = np - 1;
   if (i == 0) { p = r; q = mod; }
@@ -44,17 +49,21 @@ struct Rot {
   typename traits<T>::real c, th;  // th = t |g|: the norms move to a - th, b + th
   T se, sec;
   bool apply;
+  bool big;  // |g| > stol sqrt(a b): above the stage-stop tolerance
 };
 
 // Jacobi rotation from the 2x2 Gram entries (see tnc_svd.cu for the formula)
 template <typename T>
 __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename traits<T>::real b, T g,
-                                           typename traits<T>::real rtol, typename traits<T>::real noise2) {
+                                           typename traits<T>::real rtol, typename traits<T>::real noise2,
+                                           typename traits<T>::real stol = 0) {
   typedef typename traits<T>::real R;
   Rot<T> r;
   const R h = abs_(g);
+  const R sab = sqrt(a) * sqrt(b);
   // rows at the rounding-noise floor (or whose squared norm underflowed) count as converged
-  r.apply = (a > noise2) && (b > noise2) && (a > 0) && (b > 0) && (h > rtol * sqrt(a) * sqrt(b));
+  r.apply = (a > noise2) && (b > noise2) && (a > 0) && (b > 0) && (h > rtol * sab);
+  r.big = r.apply && h > stol * sab;
   if (!r.apply) { r.c = 1; r.th = 0; r.se = zero_<T>(); r.sec = zero_<T>(); return r; }
   const R tau = (b - a) / (2 * h);
   R t;
@@ -74,10 +83,11 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
 // squared norms a (of x) and *b (of y) are carried, not recomputed: only
 // g = <x, y> is reduced, and a rotation moves them to a - t|g|, b + t|g|
 // (exact in exact arithmetic; recomputed from the rows once per sweep).
+// Returns 0 (no rotation), 1 (a rotation) or 3 (a rotation above stol).
 template <typename T, int MAXE>
-__device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, typename traits<T>::real rtol,
-                                                typename traits<T>::real noise2, typename traits<T>::real& a,
-                                                typename traits<T>::real* b) {
+__device__ __forceinline__ int rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, typename traits<T>::real rtol,
+                                               typename traits<T>::real noise2, typename traits<T>::real& a,
+                                               typename traits<T>::real* b, typename traits<T>::real stol) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
   const int Li = (int)L;  // row length <= 32 * MAXE
@@ -95,8 +105,8 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
   }
   const T g = warp_sum(g0 + g1);
   const R bb = *b;
-  const Rot<T> r = make_rot<T>(a, bb, g, rtol, noise2);
-  if (!r.apply) return false;
+  const Rot<T> r = make_rot<T>(a, bb, g, rtol, noise2, stol);
+  if (!r.apply) return 0;
 #pragma unroll
   for (int u = 0; u < MAXE; ++u) {
     const int k = lane + 32 * u;
@@ -106,14 +116,15 @@ __device__ __forceinline__ bool rotate_reg_smem(T (&x)[MAXE], T* y, int64_t L, t
   }
   a = a - r.th;
   if (lane == 0) *b = bb + r.th;
-  return true;
+  return r.big ? 3 : 1;
 }
 
-// rows x and y both in shared memory, one warp; squared norms *a, *b carried
+// rows x and y both in shared memory, one warp; squared norms *a, *b carried;
+// returns as rotate_reg_smem
 template <typename T>
-__device__ __forceinline__ bool rotate_smem_smem(T* x, T* y, int64_t L, typename traits<T>::real rtol,
-                                                 typename traits<T>::real noise2, typename traits<T>::real* a,
-                                                 typename traits<T>::real* b) {
+__device__ __forceinline__ int rotate_smem_smem(T* x, T* y, int64_t L, typename traits<T>::real rtol,
+                                                typename traits<T>::real noise2, typename traits<T>::real* a,
+                                                typename traits<T>::real* b, typename traits<T>::real stol) {
   typedef typename traits<T>::real R;
   const int lane = threadIdx.x & 31;
   T g0 = zero_<T>(), g1 = zero_<T>();
@@ -125,8 +136,8 @@ __device__ __forceinline__ bool rotate_smem_smem(T* x, T* y, int64_t L, typename
   if (k < L) fma_(g0, x[k], conj_(y[k]));
   const T g = warp_sum(g0 + g1);
   const R aa = *a, bb = *b;
-  const Rot<T> r = make_rot<T>(aa, bb, g, rtol, noise2);
-  if (!r.apply) return false;
+  const Rot<T> r = make_rot<T>(aa, bb, g, rtol, noise2, stol);
+  if (!r.apply) return 0;
   for (int64_t kk = lane; kk < L; kk += 32) {
     const T xv = x[kk], yv = y[kk];
     x[kk] = r.c * xv - r.se * yv;
@@ -135,7 +146,7 @@ __device__ __forceinline__ bool rotate_smem_smem(T* x, T* y, int64_t L, typename
   __syncwarp();
   if (lane == 0) { *a = aa - r.th; *b = bb + r.th; }
   __syncwarp();
-  return true;
+  return r.big ? 3 : 1;
 }
 
 // squared norm of one row (length L) by one warp, every lane gets it
@@ -246,7 +257,8 @@ __device__ __forceinline__ dfr df_dot3(dfr c, dfr u, dfr p, dfr v, dfr q, dfr w)
 }
 
 // complex DF rows x, y in shared memory, one warp; squared norms carried
-__device__ __forceinline__ bool rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b) {
+__device__ __forceinline__ int rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b,
+                                                dfr /*stol: the finish has no stage stop*/) {
   const int lane = threadIdx.x & 31;
   // g = sum x conj(y): Re = xr yr + xi yi, Im = xi yr - xr yi, four Dot2 chains
   float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f, s3 = 0.f, c3 = 0.f;
@@ -260,7 +272,7 @@ __device__ __forceinline__ bool rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr 
   const dfr gre = warp_sum_df(df_add(df_norm(s0, c0), df_norm(s1, c1)));
   const dfr gim = warp_sum_df(df_add(df_norm(s2, c2), df_norm(s3, c3)));
   const RotDF r = make_rot_df(*a, *b, gre, gim, rtol.h, noise2.h, true);
-  if (!r.apply) return false;
+  if (!r.apply) return 0;
   if (!r.big) {
     // x += (c-1) x - se y, y += conj(se) x + (c-1) y, from the hi parts
     const float cm1 = r.cm1, ser = r.ser, sei = r.sei;
@@ -293,11 +305,12 @@ __device__ __forceinline__ bool rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr 
   __syncwarp();
   if (lane == 0) { *a = r.a; *b = r.b; }
   __syncwarp();
-  return true;
+  return 1;
 }
 
 // real DF rows
-__device__ __forceinline__ bool rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b) {
+__device__ __forceinline__ int rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b,
+                                                dfr /*stol*/) {
   const int lane = threadIdx.x & 31;
   float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
   int64_t k = lane;
@@ -309,7 +322,7 @@ __device__ __forceinline__ bool rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr 
   if (k < L) dot2_acc(s0, c0, x[k].h, x[k].l, y[k].h, y[k].l);
   const dfr g = warp_sum_df(df_add(df_norm(s0, c0), df_norm(s1, c1)));
   const RotDF r = make_rot_df(*a, *b, g, dfr(0.f, 0.f), rtol.h, noise2.h, false);
-  if (!r.apply) return false;
+  if (!r.apply) return 0;
   if (!r.big) {
     const float cm1 = r.cm1, se = r.ser;
     for (int64_t kk = lane; kk < L; kk += 32) {
@@ -331,7 +344,7 @@ __device__ __forceinline__ bool rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr 
   __syncwarp();
   if (lane == 0) { *a = r.a; *b = r.b; }
   __syncwarp();
-  return true;
+  return 1;
 }
 
 __device__ __forceinline__ dfr warp_row_norm2(const dfc* x, int64_t L) {
@@ -411,7 +424,7 @@ template <typename T, int MAXE, int MAXT, bool PREG>
 __global__ void __launch_bounds__(MAXT, jacobi_min_blocks<T, MAXE, MAXT, PREG>())
 jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double tol, const double* frob2,
                     typename traits<T>::real* Dn, unsigned* counters, unsigned* ver, SyncWords* sw, int* info,
-                    int64_t nkeep) {
+                    int64_t nkeep, double stop_tol) {
   typedef typename traits<T>::real R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sB = reinterpret_cast<T*>(smem_raw);
@@ -425,13 +438,14 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
   // take no rotation (their rows need only be orthogonal to the kept ones)
   const int64_t kb = (nkeep + h - 1) / h;
   const R rtol = (R)tol;
+  const R stol = (R)stop_tol;
   const R noise2 = noise_floor2<T>(frob2);
   int sweep = 0;
-  bool converged = false;
+  bool converged = false, staged = false;
   unsigned last_rot = 0;
   T x[PREG ? MAXE : 1];
   for (; sweep < max_sweeps; ++sweep) {
-    unsigned rot = 0;
+    unsigned rot = 0, rotb = 0;
     // step index of this sweep's phase 0; a sweep is nbp steps (phase 0 and
     // nbp - 1 rounds).  The grid barrier that ends the previous sweep has
     // ordered every earlier step, so phase 0 waits for nothing.
@@ -453,8 +467,11 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
         if (warp < hp / 2) {
           int64_t p, q;
           circle_pair(hp, rr, warp, p, q);
-          if (p < cnt && q < cnt)
-            rot += rotate_smem_smem(sB + p * L, sB + q * L, L, rtol, noise2, &sn[p], &sn[q]) ? 1u : 0u;
+          if (p < cnt && q < cnt) {
+            const int rr = rotate_smem_smem(sB + p * L, sB + q * L, L, rtol, noise2, &sn[p], &sn[q], stol);
+            rot += (unsigned)(rr & 1);
+            rotb += (unsigned)(rr >> 1);
+          }
         }
         __syncthreads();
       }
@@ -499,8 +516,11 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
           __syncthreads();
           for (int s = 0; s < h; ++s) {
             const int j = (warp + s) % h;
-            if (hasA && j < cntB)
-              rot += rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol, noise2, an, &sn[j]) ? 1u : 0u;
+            if (hasA && j < cntB) {
+              const int rr = rotate_reg_smem<T, MAXE>(x, sB + (int64_t)j * L, L, rtol, noise2, an, &sn[j], stol);
+              rot += (unsigned)(rr & 1);
+              rotb += (unsigned)(rr >> 1);
+            }
             __syncthreads();
           }
           if (hasA) {
@@ -524,11 +544,12 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
           __syncthreads();
           for (int s = 0; s < h; ++s) {
             const int j = (warp + s) % h;
-            if (warp < cntA && j < cntB)
-              rot += rotate_smem_smem(sA + (int64_t)warp * L, sB + (int64_t)j * L, L, rtol, noise2, &snA[warp],
-                                      &sn[j])
-                         ? 1u
-                         : 0u;
+            if (warp < cntA && j < cntB) {
+              const int rr = rotate_smem_smem(sA + (int64_t)warp * L, sB + (int64_t)j * L, L, rtol, noise2,
+                                              &snA[warp], &sn[j], stol);
+              rot += (unsigned)(rr & 1);
+              rotb += (unsigned)(rr >> 1);
+            }
             __syncthreads();
           }
           rows_from_smem(W, p0, cntA, L, sA);
@@ -540,14 +561,19 @@ jacobi_block_kernel(T* W, int64_t nr, int64_t L, int h, int max_sweeps, double t
       }
     }
     if (lane == 0 && rot) atomicAdd(&counters[sweep], rot);
+    if (lane == 0 && rotb) atomicAdd(&counters[kRowsMaxSweeps + sweep], rotb);
     if (!grid_barrier(sw, gridDim.x)) return;
     last_rot = ld_volatile(&counters[sweep]);
     if (last_rot == 0) { converged = true; ++sweep; break; }
+    // stage stop: no rotation of this sweep was above stop_tol (a later
+    // stage finishes the rows)
+    if (stop_tol > 0 && ld_volatile(&counters[kRowsMaxSweeps + sweep]) == 0) { staged = true; ++sweep; break; }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    info[0] = converged ? TNC_OK : TNC_ERR_NOT_CONVERGED;
+    info[0] = (converged || staged) ? TNC_OK : TNC_ERR_NOT_CONVERGED;
     info[1] = sweep;
     info[2] = (int)last_rot;
+    info[3] = staged ? 1 : 0;
   }
 }
 
@@ -603,8 +629,8 @@ inline size_t gram_smem_bytes(int64_t L) {
 // Returns the number of rotations applied.  Called by every thread.
 template <typename T>
 __device__ unsigned gram_task(T* W, int64_t nr, int64_t L, int64_t LP, T* X, T* part, GramState<T>& gs,
-                              int64_t P, int64_t Q, typename traits<T>::real rtol,
-                              typename traits<T>::real noise2) {
+                              int64_t P, int64_t Q, typename traits<T>::real rtol, typename traits<T>::real noise2,
+                              typename traits<T>::real stol, unsigned& rotb) {
   typedef typename traits<T>::real R;
   constexpr int H = kGramH, H2 = kGramRows, NE = H2 * H2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -693,9 +719,10 @@ __device__ unsigned gram_task(T* W, int64_t nr, int64_t L, int64_t LP, T* X, T* 
       }
       if (ok) {
         const T* Gc = gs.G[cur];
-        const Rot<T> r = make_rot<T>(real_(Gc[x * H2 + x]), real_(Gc[y * H2 + y]), Gc[x * H2 + y], rtol, noise2);
+        const Rot<T> r =
+            make_rot<T>(real_(Gc[x * H2 + x]), real_(Gc[y * H2 + y]), Gc[x * H2 + y], rtol, noise2, stol);
         if (r.apply) {
-          applied = 1;
+          applied = r.big ? 3 : 1;
           gs.jc[x] = r.c;
           gs.jc[y] = r.c;
           gs.jo[x] = -r.se;
@@ -705,7 +732,9 @@ __device__ unsigned gram_task(T* W, int64_t nr, int64_t L, int64_t LP, T* X, T* 
         }
       }
       const unsigned nrot = __popc(__ballot_sync(0xffffffffu, applied != 0));
+      const unsigned nbig = __popc(__ballot_sync(0xffffffffu, applied == 3));
       rot += lane == 0 ? nrot : 0u;
+      rotb += lane == 0 ? nbig : 0u;
     }
     // one barrier that also tells every thread whether anything rotated (a
     // step without rotations leaves G and U as they are; the next step's
@@ -759,7 +788,7 @@ __device__ unsigned gram_task(T* W, int64_t nr, int64_t L, int64_t LP, T* X, T* 
 template <typename T>
 __global__ void __launch_bounds__(kGramWarps * 32, 2)
 jacobi_gram_kernel(T* W, int64_t nr, int64_t L, int max_sweeps, double tol, const double* frob2, unsigned* counters,
-                   unsigned* ver, SyncWords* sw, int* info, int64_t nkeep) {
+                   unsigned* ver, SyncWords* sw, int* info, int64_t nkeep, double stop_tol) {
   typedef typename traits<T>::real R;
   constexpr int H = kGramH;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -772,15 +801,16 @@ jacobi_gram_kernel(T* W, int64_t nr, int64_t L, int max_sweeps, double tol, cons
   const int64_t ntask = nbp / 2;
   const int64_t kb = (nkeep + H - 1) / H;
   const R rtol = (R)tol;
+  const R stol = (R)stop_tol;
   const R noise2 = noise_floor2<T>(frob2);
   int sweep = 0;
-  bool converged = false;
+  bool converged = false, staged = false;
   unsigned last_rot = 0;
   for (; sweep < max_sweeps; ++sweep) {
-    unsigned rot = 0;
+    unsigned rot = 0, rotb = 0;
     const unsigned g0 = (unsigned)sweep * (unsigned)nbp;
     for (int64_t hb = blockIdx.x; hb < nb; hb += gridDim.x) {
-      if (hb < kb) rot += gram_task<T>(W, nr, L, LP, X, part, gs, hb, -1, rtol, noise2);
+      if (hb < kb) rot += gram_task<T>(W, nr, L, LP, X, part, gs, hb, -1, rtol, noise2, stol, rotb);
       publish_steps(ver, hb, hb, g0 + 1u);
     }
     for (int64_t r = 0; r < nbp - 1; ++r) {
@@ -795,19 +825,22 @@ jacobi_gram_kernel(T* W, int64_t nr, int64_t L, int max_sweeps, double tol, cons
           continue;
         }
         if (!wait_steps(ver, P, Q, g, sw)) return;
-        if (!(P >= kb && Q >= kb)) rot += gram_task<T>(W, nr, L, LP, X, part, gs, P, Q, rtol, noise2);
+        if (!(P >= kb && Q >= kb)) rot += gram_task<T>(W, nr, L, LP, X, part, gs, P, Q, rtol, noise2, stol, rotb);
         publish_steps(ver, P, Q, g + 1u);
       }
     }
     if (threadIdx.x == 0 && rot) atomicAdd(&counters[sweep], rot);
+    if (threadIdx.x == 0 && rotb) atomicAdd(&counters[kRowsMaxSweeps + sweep], rotb);
     if (!grid_barrier(sw, gridDim.x)) return;
     last_rot = ld_volatile(&counters[sweep]);
     if (last_rot == 0) { converged = true; ++sweep; break; }
+    if (stop_tol > 0 && ld_volatile(&counters[kRowsMaxSweeps + sweep]) == 0) { staged = true; ++sweep; break; }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    info[0] = converged ? TNC_OK : TNC_ERR_NOT_CONVERGED;
+    info[0] = (converged || staged) ? TNC_OK : TNC_ERR_NOT_CONVERGED;
     info[1] = sweep;
     info[2] = (int)last_rot;
+    info[3] = staged ? 1 : 0;
   }
 }
 
@@ -881,7 +914,6 @@ __global__ void wait_selftest_kernel(int kind, SyncWords* sw, unsigned* ver, int
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct RowsLayout { size_t d, dn, frob2, counters, sync, total; };
-static const int kRowsMaxSweeps = 100;
 static RowsLayout rows_layout(int64_t nr, size_t rs) {
   RowsLayout Ly;
   size_t off = 0;
@@ -889,7 +921,7 @@ static RowsLayout rows_layout(int64_t nr, size_t rs) {
   Ly.dn = off; off = align256(off + (size_t)nr * rs);
   Ly.frob2 = off; off = align256(off + sizeof(double));
   // sweep rotation counters, then one step counter per half-block (<= nr)
-  Ly.counters = off; off = align256(off + (kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned));
+  Ly.counters = off; off = align256(off + (2 * kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned));
   Ly.sync = off; off = align256(off + sizeof(SyncWords));
   Ly.total = off;
   return Ly;
@@ -923,7 +955,7 @@ static int ensure_smem_attr() {
 template <typename T, int MAXE, int MAXT, bool PREG = true>
 static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, const double* frob2,
                         typename traits<T>::real* Dn, unsigned* counters, SyncWords* sw, int* info, int64_t nkeep,
-                        cudaStream_t st) {
+                        cudaStream_t st, double stop_tol = 0.0) {
   const size_t smem = (size_t)(PREG ? 1 : 2) * h * L * sizeof(T);
   const void* fn = (const void*)jacobi_block_kernel<T, MAXE, MAXT, PREG>;
   if (smem > kMaxHalfBlockBytes || 32 * h > MAXT) return TNC_ERR_ARG;
@@ -938,20 +970,21 @@ static int launch_block(T* W, int64_t nr, int64_t L, int h, int ms, double tol, 
   int64_t want = ntask;
   if (want < 1) want = 1;
   int grid = (int)(want < cap ? want : cap);
-  unsigned* ver = counters + kRowsMaxSweeps;
+  unsigned* ver = counters + 2 * kRowsMaxSweeps;
   int64_t nr_ = nr, L_ = L;
   int h_ = h, ms_ = ms;
   double tol_ = tol;
   int64_t nkeep_ = nkeep;
-  void* args[] = {(void*)&W,  (void*)&nr_, (void*)&L_,       (void*)&h_,  (void*)&ms_, (void*)&tol_,   (void*)&frob2,
-                  (void*)&Dn, (void*)&counters, (void*)&ver, (void*)&sw, (void*)&info, (void*)&nkeep_};
+  double stop_ = stop_tol;
+  void* args[] = {(void*)&W,  (void*)&nr_,      (void*)&L_,  (void*)&h_,  (void*)&ms_,   (void*)&tol_,    (void*)&frob2,
+                  (void*)&Dn, (void*)&counters, (void*)&ver, (void*)&sw,  (void*)&info,  (void*)&nkeep_,  (void*)&stop_};
   if (cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, st) != cudaSuccess) return TNC_ERR_CUDA;
   return TNC_OK;
 }
 
 template <typename T>
 static int launch_gram(T* W, int64_t nr, int64_t L, int ms, double tol, const double* frob2, unsigned* counters,
-                       SyncWords* sw, int* info, int64_t nkeep, cudaStream_t st) {
+                       SyncWords* sw, int* info, int64_t nkeep, cudaStream_t st, double stop_tol) {
   const size_t smem = gram_smem_bytes<T>(L);
   const void* fn = (const void*)jacobi_gram_kernel<T>;
   if (smem > kMaxHalfBlockBytes) return TNC_ERR_ARG;
@@ -973,12 +1006,12 @@ static int launch_gram(T* W, int64_t nr, int64_t L, int ms, double tol, const do
   const int64_t nb = (nr + kGramH - 1) / kGramH;
   const int64_t ntask = (nb + (nb & 1)) / 2;
   const int grid = (int)(ntask < cap ? (ntask < 1 ? 1 : ntask) : cap);
-  unsigned* ver = counters + kRowsMaxSweeps;
+  unsigned* ver = counters + 2 * kRowsMaxSweeps;
   int64_t nr_ = nr, L_ = L, nkeep_ = nkeep;
   int ms_ = ms;
-  double tol_ = tol;
-  void* args[] = {(void*)&W,        (void*)&nr_, (void*)&L_,  (void*)&ms_,  (void*)&tol_,  (void*)&frob2,
-                  (void*)&counters, (void*)&ver, (void*)&sw,  (void*)&info, (void*)&nkeep_};
+  double tol_ = tol, stop_ = stop_tol;
+  void* args[] = {(void*)&W,        (void*)&nr_, (void*)&L_,  (void*)&ms_,  (void*)&tol_,   (void*)&frob2,
+                  (void*)&counters, (void*)&ver, (void*)&sw,  (void*)&info, (void*)&nkeep_, (void*)&stop_};
   if (cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, st) != cudaSuccess) return TNC_ERR_CUDA;
   return TNC_OK;
 }
@@ -986,7 +1019,7 @@ static int launch_gram(T* W, int64_t nr, int64_t L, int ms, double tol, const do
 template <typename T>
 static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits<T>::real* S, int64_t* order,
                          int max_sweeps, double tol, int block_rows, int64_t nkeep, void* work, size_t wb, int* info,
-                         cudaStream_t st) {
+                         cudaStream_t st, double stop_tol = 0.0) {
   typedef typename traits<T>::real R;
   if (m <= 0 || n <= 0 || !A || !W || !S || !order || !work || !info) return TNC_ERR_ARG;
   const int tall = m > n;
@@ -1013,7 +1046,7 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
                                                                                                       : TNC_ERR_CUDA;
   }
   if (s) return s;
-  if (cudaMemsetAsync(counters, 0, (kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned), st) != cudaSuccess)
+  if (cudaMemsetAsync(counters, 0, (2 * kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned), st) != cudaSuccess)
     return TNC_ERR_CUDA;
   if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(info, 0, 4 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
@@ -1038,26 +1071,27 @@ static int svd_rows_impl(int64_t m, int64_t n, const T* A, T* W, typename traits
                       gram_smem_bytes<T>(L) <= kMaxHalfBlockBytes;
     int rc;
     if (gram) {
-      if constexpr (sizeof(R) == 4) rc = launch_gram<T>(W, nr, L, max_sweeps, tol, frob2, counters, sw, info, nkeep, st);
+      if constexpr (sizeof(R) == 4)
+        rc = launch_gram<T>(W, nr, L, max_sweeps, tol, frob2, counters, sw, info, nkeep, st, stop_tol);
       else return TNC_ERR_ARG;
     } else if (sizeof(typename traits<T>::real) == 8 && L <= 512) {
       // FP64 rows: both half-blocks in shared memory (2 h L elements)
       if (h > 8) h = 8;
       while (h > 2 && (size_t)2 * h * L * sizeof(T) > kMaxHalfBlockBytes) h >>= 1;
-      rc = launch_block<T, 1, 256, false>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
+      rc = launch_block<T, 1, 256, false>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st, stop_tol);
     } else if (h == 16) {
       if constexpr (sizeof(T) <= 8) {
-        if (L <= 256) rc = launch_block<T, 8, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
-        else rc = launch_block<T, 16, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
+        if (L <= 256) rc = launch_block<T, 8, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st, stop_tol);
+        else rc = launch_block<T, 16, 512>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st, stop_tol);
       } else {
         return TNC_ERR_ARG;
       }
     } else if (L <= 256) {
-      rc = launch_block<T, 8, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
+      rc = launch_block<T, 8, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st, stop_tol);
     } else if (L <= 512) {
-      rc = launch_block<T, 16, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
+      rc = launch_block<T, 16, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st, stop_tol);
     } else if (L <= 1024 && !big) {
-      if constexpr (sizeof(T) < 16) rc = launch_block<T, 32, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st);
+      if constexpr (sizeof(T) < 16) rc = launch_block<T, 32, 256>(W, nr, L, h, max_sweeps, tol, frob2, Dn, counters, sw, info, nkeep, st, stop_tol);
       else return TNC_ERR_ARG;
     } else {
       return TNC_ERR_ARG;  // rows too long for the register-resident half block
@@ -1195,7 +1229,7 @@ static int svd_rows_df_impl(int64_t m, int64_t n, const Tin* A, void* Wv, double
   SyncWords* sw = (SyncWords*)(w + Ly.sync);
   double* frob2 = (double*)(w + Ly.frob2);  // [0] of A, [1] of the scaled rows
   Tdf* W = (Tdf*)Wv;
-  if (cudaMemsetAsync(counters, 0, (kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned), st) != cudaSuccess)
+  if (cudaMemsetAsync(counters, 0, (2 * kRowsMaxSweeps + (size_t)nr) * sizeof(unsigned), st) != cudaSuccess)
     return TNC_ERR_CUDA;
   if (cudaMemsetAsync(sw, 0, sizeof(SyncWords), st) != cudaSuccess) return TNC_ERR_CUDA;
   if (cudaMemsetAsync(info, 0, 4 * sizeof(int), st) != cudaSuccess) return TNC_ERR_CUDA;
@@ -1252,6 +1286,17 @@ extern "C" int tnc_svd_rows_keep(int dtype, int64_t m, int64_t n, const void* A,
   TNC_DISPATCH(dtype, T,
                return svd_rows_impl<T>(m, n, (const T*)A, (T*)W, (typename traits<T>::real*)S, order, max_sweeps,
                                        tol, block_rows, nkeep, work, work_bytes, info, st));
+  return TNC_ERR_ARG;
+}
+
+extern "C" int tnc_svd_rows_stage(int dtype, int64_t m, int64_t n, const void* A, void* W, void* S, int64_t* order,
+                                  int max_sweeps, double tol, double stop_tol, int block_rows, void* work,
+                                  size_t work_bytes, int* info, void* stream) {
+  if (!(stop_tol >= 0.0)) return TNC_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  TNC_DISPATCH(dtype, T,
+               return svd_rows_impl<T>(m, n, (const T*)A, (T*)W, (typename traits<T>::real*)S, order, max_sweeps,
+                                       tol, block_rows, INT64_MAX, work, work_bytes, info, st, stop_tol));
   return TNC_ERR_ARG;
 }
 

@@ -81,6 +81,12 @@ struct Dims {
 constexpr double kCoreFp32Tol = 3e-6;
 constexpr int kCoreFp32Sweeps = 14;
 constexpr double kCoreTol = 1e-7;
+// The FP32 stage of a finished core also stops after the first sweep whose
+// rotations were all below kCoreStopTol relative: the finish converges the
+// rows from there and confirms their orthogonality itself, so the FP32
+// stage's own checking sweep (and its last sweeps at the rounding floor)
+// are not needed.
+constexpr double kCoreStopTol = 1e-3;
 // Rows beyond the FP32 stage's retained rank that the FP64 stage still
 // finishes against each other: the FP64 decision may retain a few more (or
 // rank them differently); if it retains any row beyond, the whole finish
@@ -400,8 +406,9 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
     const bool core_path = P.core64 && rows_path && m <= core_rows_limit(dt);
     if (rows_path) {
       if (tnc_svd_rows_workspace_size(dt, kmin, m, &xb) != TNC_OK || xb > factb) return TNC_ERR_WORKSPACE;
-      if (int rc = tnc_svd_rows(dt, kmin, m, B.rbuf, B.wbuf, B.S, B.order, core_path ? kCoreFp32Sweeps : 0,
-                                core_path ? kCoreFp32Tol : 0.0, block_rows, B.fact, factb, B.info, st))
+      if (int rc = tnc_svd_rows_stage(dt, kmin, m, B.rbuf, B.wbuf, B.S, B.order, core_path ? kCoreFp32Sweeps : 0,
+                                      core_path ? kCoreFp32Tol : 0.0, core_path ? kCoreStopTol : 0.0, block_rows,
+                                      B.fact, factb, B.info, st))
         return rc;
     } else {  // the accumulating SVD of R: its VH rows are U^H of M
       if (tnc_svd_workspace_size(dt, kmin, m, &xb) != TNC_OK || xb > factb) return TNC_ERR_WORKSPACE;

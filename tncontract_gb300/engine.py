@@ -142,6 +142,8 @@ def _check_info(info):
 # tolerances of the storage-precision Jacobi stage and of the finishing
 # (double-float or FP64) stage, as in the native sweep (tnc_sweep.cu)
 CORE_FP32_TOL, CORE_FP32_SWEEPS, CORE_FP64_TOL = 3e-6, 14, 1e-7
+# the FP32 stage also stops after a sweep whose rotations were all below this
+CORE_STOP_TOL = 1e-3
 _WIDE = {torch.float32: torch.float64, torch.complex64: torch.complex128}
 
 
@@ -174,7 +176,7 @@ def _factor_full(M, core=None):
         # the double-float (or FP64) Jacobi finishes the rows; S, the rank
         # decision and U come from the finished rows, U is stored back in the
         # sites' precision
-        W32, _s, _o, info = _ops.svd_rows(R, max_sweeps=CORE_FP32_SWEEPS, tol=CORE_FP32_TOL)
+        W32, _s, _o, info = _ops.svd_rows_stage(R, CORE_FP32_SWEEPS, CORE_FP32_TOL, CORE_STOP_TOL)
         if int(info[0].item()) not in (L.OK, L.ERR_NOT_CONVERGED):
             _check_info(info)
         if core == "df":
