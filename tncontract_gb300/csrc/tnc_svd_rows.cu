@@ -413,7 +413,10 @@ __device__ __forceinline__ bool wait_steps(const unsigned* ver, int64_t P, int64
 // on the same SM (a register-resident FP64 row took all 255 registers a
 // thread, so nothing else could share the SM).  Double-float rows fill the
 // shared memory of an SM with one CTA (2 x 8 rows of 512 16-byte elements)
-// and keep the registers of their Dot2 chains.
+// and keep the registers of their Dot2 chains (held to 128 registers the
+// complex kernel spills 144 bytes and took 6.8 against 4.8 ms at 512 x 512;
+// the sweep fell from 4.98 to 4.54 sweeps/s although an FP32 CTA then fits
+// beside it).
 template <typename T, int MAXE, int MAXT, bool PREG>
 constexpr int jacobi_min_blocks() {
   if (std::is_same<T, dfc>::value || std::is_same<T, dfr>::value) return 1;
