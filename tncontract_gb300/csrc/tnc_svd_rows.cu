@@ -54,9 +54,9 @@ struct Rot {
 
 // Jacobi rotation from the 2x2 Gram entries (see tnc_svd.cu for the formula)
 template <typename T>
-__device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename traits<T>::real b, T g,
-                                           typename traits<T>::real rtol, typename traits<T>::real noise2,
-                                           typename traits<T>::real stol = 0) {
+__device__ __forceinline__ Rot<T> make_rot_ieee(typename traits<T>::real a, typename traits<T>::real b, T g,
+                                                typename traits<T>::real rtol, typename traits<T>::real noise2,
+                                                typename traits<T>::real stol) {
   typedef typename traits<T>::real R;
   Rot<T> r;
   const R h = abs_(g);
@@ -77,6 +77,51 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
   r.se = s * e;
   r.sec = s * conj_(e);
   return r;
+}
+
+// The same rotation for single-precision rows with a shorter dependency
+// chain (the rotation parameters are on the critical path of every Jacobi
+// step): the tests compare squares (|g|^2 > tol^2 a b, no square roots),
+// 1/|g| is one correctly rounded reciprocal square root instead of a hypot
+// and a division, and the divisions of tau, t and c become a product and
+// correctly rounded reciprocals.  Every rounding stays round-to-nearest, so
+// the rotations carry no systematic bias (|e| = 1 and c^2 + s^2 = 1 to an
+// ulp either side; a Newton-refined hardware estimate here drifted the FP32
+// sweep's discarded weights by 1.5e-6).  Operands whose squares or products
+// leave the comfortable FP32 range take the IEEE formula.
+template <typename T>
+__device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename traits<T>::real b, T g,
+                                           typename traits<T>::real rtol, typename traits<T>::real noise2,
+                                           typename traits<T>::real stol = 0) {
+  typedef typename traits<T>::real R;
+  if constexpr (sizeof(R) != 4) {
+    return make_rot_ieee<T>(a, b, g, rtol, noise2, stol);
+  } else {
+    const float h2 = abs2_(g), ab = a * b;
+    if (!(h2 > 1e-30f && h2 < 1e30f && ab > 1e-30f && ab < 1e30f))
+      return make_rot_ieee<T>(a, b, g, rtol, noise2, stol);
+    Rot<T> r;
+    r.apply = (a > noise2) && (b > noise2) && (h2 > (rtol * rtol) * ab);
+    r.big = r.apply && h2 > (stol * stol) * ab;
+    if (!r.apply) { r.c = 1; r.th = 0; r.se = zero_<T>(); r.sec = zero_<T>(); return r; }
+    const float ih = __frsqrt_rn(h2);  // 1 / |g|
+    const float tau = (b - a) * 0.5f * ih;
+    const float at = fabsf(tau);
+    float t;
+    if (at > 1e15f) {
+      t = 0.5f / tau;
+    } else {
+      t = copysignf(__frcp_rn(at + sqrtf(fmaf(tau, tau, 1.f))), tau);
+    }
+    const float c = __frcp_rn(sqrtf(fmaf(t, t, 1.f)));
+    const float s = c * t;
+    r.c = c;
+    r.th = t * (h2 * ih);
+    const T e = g * ih;
+    r.se = s * e;
+    r.sec = s * conj_(e);
+    return r;
+  }
 }
 
 // rows x (registers, MAXE per lane) and y (shared memory), one warp.  The
