@@ -334,7 +334,9 @@ int tnc_permute_rows(int dtype, int64_t n, int64_t L, const void *src,
  * scaled by a power of two to unit Frobenius norm inside; W (m x n) receives
  * the orthogonalised rows as FP64 / complex128 elements, S (FP64) and order
  * as tnc_svd_rows for the FP64 type, and the rows are orthogonal to tol
- * relative (<= 0: 1e-7).  Rows beyond nkeep as in tnc_svd_rows_keep.  Rows
+ * relative (<= 0: 1e-7).  The finish ends without a checking sweep (info[3]
+ * = 1) after a rotating sweep whose rotations were all small angles below
+ * 1e-5 relative: their residual is second order (about 1e-8).  Rows beyond nkeep as in tnc_svd_rows_keep.  Rows
  * up to 800 complex / 1600 real elements.  Workspace:
  * tnc_svd_rows_workspace_size of the FP64 type.  Replaces, in the sweep,
  * the FP64 finish (tnc_cast to the FP64 type + tnc_svd_rows_keep). */

@@ -247,18 +247,23 @@ __device__ __forceinline__ void rows_from_smem(T* W, int64_t row0, int cnt, int6
 // product.
 struct RotDF {
   bool apply, big;
+  bool above;           // a large angle, or |g| above the stop tolerance
   float cm1, ser, sei;  // small angle: c - 1 and s e (e = g / |g|)
   dfr c, sr, si;        // large angle: c and s e
   dfr a, b;             // the rows' new squared norms
 };
 
-__device__ __forceinline__ RotDF make_rot_df(dfr a, dfr b, dfr gre, dfr gim, float rtol, float noise2, bool cplx) {
+__device__ __forceinline__ RotDF make_rot_df(dfr a, dfr b, dfr gre, dfr gim, float rtol, float noise2, bool cplx,
+                                             float stol) {
   RotDF r;
   r.apply = false;
   r.big = false;
+  r.above = false;
   const float gabs = cplx ? hypotf(gre.h, gim.h) : fabsf(gre.h);
+  const float sab = sqrtf(a.h) * sqrtf(b.h);
   // rows at the rounding-noise floor count as converged (as make_rot)
-  if (!(a.h > noise2 && b.h > noise2 && gabs > rtol * sqrtf(a.h) * sqrtf(b.h))) return r;
+  if (!(a.h > noise2 && b.h > noise2 && gabs > rtol * sab)) return r;
+  r.above = gabs > stol * sab;
   float ds, de;
   two_sum(b.h, -a.h, ds, de);
   de = __fadd_rn(de, __fsub_rn(b.l, a.l));
@@ -278,6 +283,7 @@ __device__ __forceinline__ RotDF make_rot_df(dfr a, dfr b, dfr gre, dfr gim, flo
     r.b = df_add(b, dfr(th, 0.f));
     return r;
   }
+  r.above = true;
   const double ad = to_double(a), bd = to_double(b);
   const double gr = to_double(gre), gi = cplx ? to_double(gim) : 0.0;
   const double h = cplx ? hypot(gr, gi) : fabs(gr);
@@ -303,7 +309,7 @@ __device__ __forceinline__ dfr df_dot3(dfr c, dfr u, dfr p, dfr v, dfr q, dfr w)
 
 // complex DF rows x, y in shared memory, one warp; squared norms carried
 __device__ __forceinline__ int rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b,
-                                                dfr /*stol: the finish has no stage stop*/) {
+                                                dfr stol) {
   const int lane = threadIdx.x & 31;
   // g = sum x conj(y): Re = xr yr + xi yi, Im = xi yr - xr yi, four Dot2 chains
   float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f, s3 = 0.f, c3 = 0.f;
@@ -316,7 +322,7 @@ __device__ __forceinline__ int rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr r
   }
   const dfr gre = warp_sum_df(df_add(df_norm(s0, c0), df_norm(s1, c1)));
   const dfr gim = warp_sum_df(df_add(df_norm(s2, c2), df_norm(s3, c3)));
-  const RotDF r = make_rot_df(*a, *b, gre, gim, rtol.h, noise2.h, true);
+  const RotDF r = make_rot_df(*a, *b, gre, gim, rtol.h, noise2.h, true, stol.h);
   if (!r.apply) return 0;
   if (!r.big) {
     // x += (c-1) x - se y, y += conj(se) x + (c-1) y, from the hi parts
@@ -350,12 +356,12 @@ __device__ __forceinline__ int rotate_smem_smem(dfc* x, dfc* y, int64_t L, dfr r
   __syncwarp();
   if (lane == 0) { *a = r.a; *b = r.b; }
   __syncwarp();
-  return 1;
+  return r.above ? 3 : 1;
 }
 
 // real DF rows
 __device__ __forceinline__ int rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr rtol, dfr noise2, dfr* a, dfr* b,
-                                                dfr /*stol*/) {
+                                                dfr stol) {
   const int lane = threadIdx.x & 31;
   float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
   int64_t k = lane;
@@ -366,7 +372,7 @@ __device__ __forceinline__ int rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr r
   }
   if (k < L) dot2_acc(s0, c0, x[k].h, x[k].l, y[k].h, y[k].l);
   const dfr g = warp_sum_df(df_add(df_norm(s0, c0), df_norm(s1, c1)));
-  const RotDF r = make_rot_df(*a, *b, g, dfr(0.f, 0.f), rtol.h, noise2.h, false);
+  const RotDF r = make_rot_df(*a, *b, g, dfr(0.f, 0.f), rtol.h, noise2.h, false, stol.h);
   if (!r.apply) return 0;
   if (!r.big) {
     const float cm1 = r.cm1, se = r.ser;
@@ -389,7 +395,7 @@ __device__ __forceinline__ int rotate_smem_smem(dfr* x, dfr* y, int64_t L, dfr r
   __syncwarp();
   if (lane == 0) { *a = r.a; *b = r.b; }
   __syncwarp();
-  return 1;
+  return r.above ? 3 : 1;
 }
 
 __device__ __forceinline__ dfr warp_row_norm2(const dfc* x, int64_t L) {
@@ -1221,6 +1227,16 @@ static int sort_rows_impl(int64_t m, int64_t L, const T* src, T* dst, int64_t* o
 }
 
 // ------------------------------------------------------------ DF finish
+// The finish ends after a rotating sweep whose rotations were all small
+// angles (|t| < 2^-12) below kDfStopTol relative, without a checking sweep:
+// every rotation zeroes its pair's inner product to DF precision, and a later
+// rotation of the same sweep puts back at most |t| eps <= 2^-12 1e-5 ~ 2.4e-9
+// (|<x, z>| / |x||z| <= eps) of it -- a residual of order 1e-8 after the ~2n
+// later rotations of the two rows, below the 1e-7 tolerance and the FP32
+// rounding of the stored result.  A sweep with a large angle (two rows of
+// nearly equal norm) is followed by a checking sweep as before.
+constexpr double kDfStopTol = 1e-5;
+
 // Exponent k with |A|_F about 2^k: the DF rows are A 2^-k, inside FP32's range.
 __device__ __forceinline__ int df_scale_exp(const double* f2) {
   const double f = f2[0];
@@ -1292,7 +1308,7 @@ static int svd_rows_df_impl(int64_t m, int64_t n, const Tin* A, void* Wv, double
     while (h > 2 && h / 2 >= nr) h >>= 1;
     if ((size_t)2 * h * L * sizeof(Tdf) > kMaxHalfBlockBytes) return TNC_ERR_ARG;  // rows too long
     if (int rc = launch_block<Tdf, 1, 256, false>(W, nr, L, h, max_sweeps, tol, frob2 + 1, Dn, counters, sw, info,
-                                                 nkeep, st))
+                                                 nkeep, st, kDfStopTol))
       return rc;
     ++launched;
   }

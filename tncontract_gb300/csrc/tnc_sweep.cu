@@ -460,17 +460,19 @@ int sweep_impl(int dt, int n_sites, int64_t d, const void* const* sites, const i
         if (cudaMemcpyAsync(ord.data(), B.order64, (size_t)kmin * sizeof(int64_t), cudaMemcpyDeviceToHost, st) !=
             cudaSuccess)
           return TNC_ERR_CUDA;
-        int hinfo[2] = {0, 0};
+        int hinfo[4] = {0, 0, 0, 0};
         if (cudaMemcpyAsync(hinfo, B.info, sizeof(hinfo), cudaMemcpyDeviceToHost, st) != cudaSuccess)
           return TNC_ERR_CUDA;
         if (cudaStreamSynchronize(st) != cudaSuccess) return TNC_ERR_CUDA;
         if (hinfo[0]) return hinfo[0];
-        {  // executed arithmetic: rotating sweeps, then the checking one (pairs of kept rows);
-           // FP64 flops, or the FP32 operations of the double-float finish
+        {  // executed arithmetic: rotating sweeps, then the checking one unless the finish
+           // stopped without it (info[3]) (pairs of kept rows); FP64 flops, or the FP32
+           // operations of the double-float finish
           const double pairs = (double)kmin * kmin - (double)(kmin - nkeep) * (kmin - nkeep);
           const double nn = pairs * m, sweeps = hinfo[1] > 0 ? hinfo[1] : 1;
-          if (P.core_df) fp64_flops += ((sweeps - 1.0) * (cplx ? 44.0 : 15.0) + (cplx ? 24.0 : 6.0)) * nn;
-          else fp64_flops += ((sweeps - 1.0) * 14.0 + 4.0) * nn / (cplx ? 1.0 : 3.0);
+          const double rotating = hinfo[3] ? sweeps : sweeps - 1.0, checking = hinfo[3] ? 0.0 : 1.0;
+          if (P.core_df) fp64_flops += (rotating * (cplx ? 44.0 : 15.0) + checking * (cplx ? 24.0 : 6.0)) * nn;
+          else fp64_flops += (rotating * 14.0 + checking * 4.0) * nn / (cplx ? 1.0 : 3.0);
         }
         // the FP64 decision must retain only rows the FP64 stage finished
         const int64_t k64 = rank_rule<double>(sd, chi, threshold, eps);
