@@ -82,9 +82,8 @@ __device__ __forceinline__ Rot<T> make_rot_ieee(typename traits<T>::real a, type
 // The same rotation for single-precision rows with a shorter dependency
 // chain (the rotation parameters are on the critical path of every Jacobi
 // step): the tests compare squares (|g|^2 > tol^2 a b, no square roots),
-// 1/|g| is one correctly rounded reciprocal square root instead of a hypot
-// and a division, and the divisions of tau, t and c become a product and
-// correctly rounded reciprocals.  Every rounding stays round-to-nearest, so
+// |g| is one square root of |g|^2 instead of a hypot, and the divisions of
+// 1/|g|, tau, t and c become a product and correctly rounded reciprocals.  Every rounding stays round-to-nearest, so
 // the rotations carry no systematic bias (|e| = 1 and c^2 + s^2 = 1 to an
 // ulp either side; a Newton-refined hardware estimate here drifted the FP32
 // sweep's discarded weights by 1.5e-6).  Operands whose squares or products
@@ -104,7 +103,11 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
     r.apply = (a > noise2) && (b > noise2) && (h2 > (rtol * rtol) * ab);
     r.big = r.apply && h2 > (stol * stol) * ab;
     if (!r.apply) { r.c = 1; r.th = 0; r.se = zero_<T>(); r.sec = zero_<T>(); return r; }
-    const float ih = __frsqrt_rn(h2);  // 1 / |g|
+    // |g| and 1/|g| by correctly rounded FP32 operations (sqrt.rn, rcp.rn):
+    // a correctly rounded reciprocal square root has no FP32 instruction and
+    // would be emulated on GB300's slow FP64 pipe
+    const float hg = sqrtf(h2);
+    const float ih = __frcp_rn(hg);
     const float tau = (b - a) * 0.5f * ih;
     const float at = fabsf(tau);
     float t;
@@ -116,7 +119,7 @@ __device__ __forceinline__ Rot<T> make_rot(typename traits<T>::real a, typename 
     const float c = __frcp_rn(sqrtf(fmaf(t, t, 1.f)));
     const float s = c * t;
     r.c = c;
-    r.th = t * (h2 * ih);
+    r.th = t * hg;
     const T e = g * ih;
     r.se = s * e;
     r.sec = s * conj_(e);
