@@ -261,3 +261,28 @@ def test_tensor_svd_retry_contract_host():
         assert any("retrying" in str(r.message) for r in rec)
         from tncontract_gb300 import tensor as T
         assert calls == [T.SVD_SWEEPS, T.SVD_RETRY_SWEEPS]
+
+
+def test_committed_svd_rows_tuning():
+    """The committed tuning table (tncontract_gb300/svd_rows_tuning.json,
+    generated on a GB300 by tuning.generate): every bucket of the row
+    kernels has a choice among the candidates; lookups round rows and
+    length up to the next bucket and give None beyond the largest."""
+    from tncontract_gb300 import tuning
+    from tncontract_gb300 import _lib as L
+    tab = tuning.load()
+    assert tab, "svd_rows_tuning.json missing or empty"
+    cands = {L.ROWS_GRAM, 4, 8}
+    for name in tuning.DTYPES:
+        for n in tuning.LENGTHS:
+            if n > tuning.MAX_LEN[name]:
+                continue
+            for r in tuning.ROWS:
+                if r <= n:
+                    assert tab.get("%s:%d:%d" % (name, r, n)) in cands, (name, r, n)
+    assert tuning.key("complex64", 300, 700) == "complex64:512:1024"
+    assert tuning.key("complex64", 16, 64) == "complex64:16:64"
+    assert tuning.key("float64", 16, 2000) is None
+    fake = {"complex64:512:512": 4}
+    assert tuning.lookup("complex64", 400, 500, table=fake) == 4
+    assert tuning.lookup("complex64", 400, 600, table=fake) is None

@@ -724,12 +724,15 @@ def tune_svd_rows(M, max_sweeps=0, tol=0.0):
 def svd_rows(M, max_sweeps=0, tol=0.0, block_rows=None):
     """Jacobi stage of the sweep SVD (``tnc_svd_rows``): returns (W, S,
     order, info) with W = orthogonalised rows of M (wide) or M^H (tall).
-    ``block_rows`` None = the autotuned half-block height for this shape."""
+    ``block_rows`` None = the committed tuning table's choice for this
+    shape's bucket (``tuning.lookup``), else the run-time autotuner's."""
     M = M.contiguous()
     m, n = M.shape
     nr, Lr = min(m, n), max(m, n)
     if block_rows is None:
-        block_rows = _TUNE.get((M.dtype, m, n)) or tune_svd_rows(M, max_sweeps, tol)
+        from . import tuning
+        block_rows = (tuning.lookup(str(M.dtype).replace("torch.", ""), min(m, n), max(m, n))
+                      or _TUNE.get((M.dtype, m, n)) or tune_svd_rows(M, max_sweeps, tol))
     W = empty((nr, Lr), M.dtype)
     S = empty((nr,), real_dtype(M.dtype))
     order = torch.empty(nr, dtype=torch.int64, device=device())
