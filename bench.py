@@ -705,8 +705,9 @@ def run_learned(args):
     own MLP kernels on spectra of plain sweeps of configs 1-3
     (``learned.train_rank_model``); then the sweep runs without it (full SVD
     at every bond) and with it (randomized SVD sized by the prediction,
-    oversampling 16, 2 power iterations, the full SVD as fallback and judge),
-    and once in FP64 as the reference both are compared with.  One step =
+    oversampling 16, 2 power iterations, the full SVD as fallback when the
+    sketch fails its residual check), and once in FP64 as the reference both
+    are compared with.  One step =
     one sweep; sweeps/s with and without the predictor, the fallback rate and
     the fidelity errors are reported."""
     import numpy as np

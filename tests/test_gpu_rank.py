@@ -1,7 +1,8 @@
 """Learned rank predictor on the GPU: the MLP's forward/backward/Adam kernels
 against the float64 oracle (oracle/mlp_oracle.py), the Gaussian sketch
 generator, and what the trained predictor gains in the truncating sweep
-(randomized SVD sized by the prediction, full SVD as fallback and judge)."""
+(randomized SVD sized by the prediction, the full SVD as fallback when the
+sketch fails its residual check)."""
 import numpy as np
 import pytest
 import torch
