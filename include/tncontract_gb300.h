@@ -315,14 +315,16 @@ int tnc_svd_rows_stage(int dtype, int64_t m, int64_t n, const void *A, void *W,
 /* The rows of src (m x L) in decreasing-norm order: dst[i] = src[order[i]],
  * stable (equal norms keep their order; a NaN norm ranks last), rank[j] =
  * the dst row of src row j.  norms2: m doubles of the caller's device memory
- * (the squared norms).  src and dst must not overlap.  The sweep sorts each
+ * (the squared norms).  src and dst must not overlap; m <= 65536 (the
+ * ranking compares every pair of rows).  The sweep sorts each
  * bond matrix's rows before the R-only QR of M^H (a static column pivoting
  * of that QR: the Jacobi on R then needs fewer sweeps) -- part of the
  * truncating SVD of left_canonise, onedim_core.py:317-343. */
 int tnc_sort_rows(int dtype, int64_t m, int64_t L, const void *src, void *dst,
                   int64_t *order, int64_t *rank, double *norms2, void *stream);
-/* dst[i] = src[idx[i]] for i < n (rows of length L; device idx) -- e.g. the
- * inverse of tnc_sort_rows with idx = rank.  src and dst must not overlap. */
+/* dst[i] = src[idx[i]] for i < n (rows of length L; device idx, every
+ * value a row of src: the kernel does not check it) -- e.g. the inverse of
+ * tnc_sort_rows with idx = rank.  src and dst must not overlap. */
 int tnc_permute_rows(int dtype, int64_t n, int64_t L, const void *src,
                      const int64_t *idx, void *dst, void *stream);
 

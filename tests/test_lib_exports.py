@@ -70,6 +70,7 @@ def test_argument_checks_before_any_launch(lib):
     assert L.tnc_svd_rows_keep(lib.C64, 8, 16, d, d, d, d, 0, 0.0, 0, -1, ws, sz.value, d, None) == lib.ERR_ARG
     # row sort: source and destination the same buffer; permute: negative count, aliasing
     assert L.tnc_sort_rows(lib.C64, 8, 16, d, d, d, d, d, None) == lib.ERR_ARG
+    assert L.tnc_sort_rows(lib.C64, (1 << 16) + 1, 16, d, ws, d, d, d, None) == lib.ERR_ARG
     assert L.tnc_permute_rows(lib.C64, -1, 16, d, d, ws, None) == lib.ERR_ARG
     assert L.tnc_permute_rows(lib.C64, 4, 16, d, d, d, None) == lib.ERR_ARG
     assert L.tnc_permute_rows(lib.C64, 0, 16, d, d, ws, None) == lib.OK  # nothing to do

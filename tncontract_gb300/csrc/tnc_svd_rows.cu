@@ -1218,10 +1218,15 @@ __global__ void permute_rows_kernel(const T* src, int64_t L, const int64_t* idx,
   }
 }
 
+// The ranking compares every pair of rows (m threads, m comparisons each):
+// bond matrices have at most a few thousand rows.
+constexpr int64_t kSortRowsMax = 1 << 16;
+
 template <typename T>
 static int sort_rows_impl(int64_t m, int64_t L, const T* src, T* dst, int64_t* order, int64_t* rank, double* norms2,
                           cudaStream_t st) {
-  if (m <= 0 || L <= 0 || !src || !dst || !order || !rank || !norms2 || (const void*)src == (void*)dst)
+  if (m <= 0 || m > kSortRowsMax || L <= 0 || !src || !dst || !order || !rank || !norms2 ||
+      (const void*)src == (void*)dst)
     return TNC_ERR_ARG;
   row_norm2_kernel<T><<<grid1d(m * 32, 256), 256, 0, st>>>(src, m, L, norms2);
   rank_desc_kernel<<<grid1d(m, 128), 128, 0, st>>>(norms2, m, order, rank);
