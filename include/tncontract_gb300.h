@@ -369,18 +369,22 @@ int tnc_gather_rows(int dtype, const void *src, int64_t L, const int64_t *order,
  * mps_bonds[n_sites+1], mpo_bonds[n_sites+1] (both ends 1); out_bonds
  * [n_sites+1] and out_offsets[n_sites] (byte offset in `work` of each
  * compressed site, (phys, out_bonds[i], out_bonds[i+1])) are written.
+ * Every bond matrix's rows are sorted by norm before the R-only QR
+ * (tnc_sort_rows; U's rows are put back after the factorisation).
  * core: TNC_CORE_STORAGE (0) factors every bond core in the storage
  * precision; TNC_CORE_FP64 (1, F32 / C64 storage only) finishes the Jacobi of
  * each core (rows up to 512 for C64, 1024 for F32) in FP64 after the
  * storage-precision Jacobi, and takes the singular values, the truncation
- * decision and U from the FP64 rows (the storage-precision stage then runs
- * to 3e-6 and at most 14 sweeps, a stall above that handing over to the FP64
- * stage); TNC_CORE_DF (2) is the same with the finish in double-float
- * arithmetic (tnc_svd_rows_df) instead of FP64.  core_tol: the FP64 stage's tolerance (<= 0: 1e-7, pairs of rows
- * orthogonal to 1e-7 relative, the rounding level of U's single-precision
- * storage; the singular values' error from it is second order).  The
- * singular values inherit the storage-precision stage's rounding (FP32-class
- * relative to s_max).  The core changes the workspace size.
+ * decision and U from the finished rows (the storage-precision stage then
+ * runs to 3e-6, at most 14 sweeps, and stops after its first sweep without a
+ * rotation above 1e-3 (tnc_svd_rows_stage), a stall handing over to the
+ * finish as well); TNC_CORE_DF (2) is the same with the finish in
+ * double-float arithmetic (tnc_svd_rows_df) instead of FP64.  core_tol: the
+ * finishing stage's tolerance (<= 0: 1e-7, pairs of rows orthogonal to 1e-7
+ * relative, the rounding level of U's single-precision storage; the
+ * singular values' error from it is second order).  The singular values
+ * inherit the storage-precision stage's rounding (FP32-class relative to
+ * s_max).  The core changes the workspace size.
  * out_discarded (HOST, may be NULL): n_sites-1 doubles, [i] = the fraction of
  * the squared singular values discarded at the bond between sites i and i+1.
  * *log_norm: in, the natural log of the input state's norm factor; out, that
